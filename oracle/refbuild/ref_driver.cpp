@@ -1,0 +1,257 @@
+// Oracle driver: runs the reference's own exact-diagonalization and lattice
+// code (compiled from its sources, see Makefile) on a small text spec and
+// writes every intermediate that the GPU path must reproduce as raw
+// little-endian arrays plus a manifest.  Test infrastructure only.
+//
+// Spec lines (whitespace separated, '#' starts a comment):
+//   gchar NAME C | gdouble NAME X | gint NAME N | gbool NAME 0/1
+//   model NAME N_SITES N_BATH                 -> ED::new_model (trivial group)
+//   el MODEL OP TYPE R C V                    -> element of operator OP (type one-body/interaction)
+//   param NAME VALUE                          -> coefficient in the instance value map
+//   instance MODEL SECTORS LABEL              -> ED::new_model_instance
+//   halfbasis L N                             -> ED_halfbasis bin list
+//   hamiltonian MODEL SECTOR TAG              -> Hamiltonian_Factorized: half-operators, x0, H.x0
+//   lanczos MODEL SECTOR TAG                  -> LanczosEigenvalue/Eigenvector from x0
+//   destroy MODEL SECTOR ORB SPIN PM TAG      -> c / c^dagger applied to x0 (factorized branch)
+//   gs LABEL TAG                              -> ED::ground_state_solve
+//   qmatrix LABEL SPIN TAG                    -> ED::Green_function_solve + ED::qmatrix
+//   gz LABEL SPIN RE IM TAG                   -> ED::Green_function(z)
+//   hyb LABEL SPIN RE IM TAG                  -> ED::hybridization_function(z)
+//   sigma LABEL SPIN RE IM TAG                -> ED::self_energy(z)
+//   omega LABEL TAG                           -> ED::Potthoff_functional (cluster part)
+#include <complex>
+#include <cstdio>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <memory>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "QCM.hpp"
+#include "lattice_model.hpp"
+#include "global_parameter.hpp"
+#include "model_instance.hpp"
+#include "qcm_ED.hpp"
+#include "Hamiltonian/Hamiltonian_Factorized.hpp"
+#include "Operators/one_body_operator.hpp"
+
+using namespace std;
+typedef complex<double> cplx;
+
+extern map<string, shared_ptr<model>> models;
+extern map<size_t, shared_ptr<model_instance_base>> model_instances;
+extern std::normal_distribution<double> normal_dis;
+extern shared_ptr<lattice_model> qcm_model;
+
+static string outdir = ".";
+static ofstream manifest;
+
+template <class T>
+static void put(const string& name, const char* dtype, const vector<size_t>& shape,
+                const T* data, size_t n) {
+  string fn = outdir + "/" + name + ".bin";
+  FILE* f = fopen(fn.c_str(), "wb");
+  if (!f) throw runtime_error("cannot write " + fn);
+  if (n) fwrite(data, sizeof(T), n, f);
+  fclose(f);
+  manifest << name << ' ' << dtype;
+  for (auto s : shape) manifest << ' ' << s;
+  manifest << '\n';
+  manifest.flush();
+}
+static void put_d(const string& name, const vector<double>& v) {
+  put(name, "f8", {v.size()}, v.data(), v.size());
+}
+static void put_scalar(const string& name, double x) { put(name, "f8", {}, &x, 1); }
+static void put_cmat(const string& name, const matrix<cplx>& m) {
+  // row-major (r, c) complex128 for numpy
+  vector<cplx> rm(m.r * m.c);
+  for (size_t i = 0; i < m.r; i++)
+    for (size_t j = 0; j < m.c; j++) rm[i * m.c + j] = m(i, j);
+  put(name, "c16", {m.r, m.c}, rm.data(), rm.size());
+}
+
+struct Spec {
+  map<string, map<string, vector<matrix_element<double>>>> elements;  // model -> op -> elems
+  map<string, map<string, string>> optype;
+  map<string, double> params;
+  set<string> ops_created;
+};
+
+static void create_ops(Spec& S, const string& model) {
+  for (auto& op : S.elements[model]) {
+    string key = model + "/" + op.first;
+    if (S.ops_created.count(key)) continue;
+    ED::new_operator(model, op.first, S.optype[model][op.first], op.second);
+    S.ops_created.insert(key);
+  }
+}
+
+static map<string, double> values_for(Spec& S, const string& model) {
+  map<string, double> v;
+  for (auto& p : S.params)
+    if (S.elements[model].count(p.first)) v[p.first] = p.second;
+  return v;
+}
+
+static void dump_halfop(const string& tag, shared_ptr<HS_half_operator<double>> h) {
+  vector<uint32_t> IJ;
+  vector<double> val;
+  for (auto& g : h->v)
+    for (auto& e : g.second) {
+      IJ.push_back(e.first);
+      IJ.push_back(e.second);
+      val.push_back(g.first);
+    }
+  put(tag + "_IJ", "u4", {val.size(), 2}, IJ.data(), IJ.size());
+  put_d(tag + "_val", val);
+  vector<uint32_t> dr;
+  vector<double> dv;
+  for (auto& d : h->diag_elem) {
+    dr.push_back((uint32_t)d.r);
+    dv.push_back(d.v);
+  }
+  put(tag + "_diag_r", "u4", {dr.size()}, dr.data(), dr.size());
+  put_d(tag + "_diag_v", dv);
+  uint32_t dim = h->dim;
+  put(tag + "_dim", "u4", {}, &dim, 1);
+}
+
+static vector<double> seeded_start(size_t dim) {
+  vector<double> x(dim);
+  random(x, normal_dis);
+  return x;
+}
+
+int main(int argc, char** argv) {
+  if (argc < 3) {
+    cerr << "usage: qcm_ref_driver SPEC OUTDIR\n";
+    return 2;
+  }
+  outdir = argv[2];
+  manifest.open(outdir + "/manifest.txt");
+  qcm_model = make_shared<lattice_model>();
+  QCM::global_parameter_init();
+  Spec S;
+  ifstream in(argv[1]);
+  string line;
+  try {
+    while (getline(in, line)) {
+      auto hash = line.find('#');
+      if (hash != string::npos) line = line.substr(0, hash);
+      istringstream ss(line);
+      string cmd;
+      if (!(ss >> cmd)) continue;
+      if (cmd == "gchar") {
+        string n; char c; ss >> n >> c; set_global_char(n, c);
+      } else if (cmd == "gdouble") {
+        string n; double x; ss >> n >> x; set_global_double(n, x);
+      } else if (cmd == "gint") {
+        string n; size_t x; ss >> n >> x; set_global_int(n, x);
+      } else if (cmd == "gbool") {
+        string n; int x; ss >> n >> x; set_global_bool(n, x != 0);
+      } else if (cmd == "model") {
+        string n; size_t ns, nb; ss >> n >> ns >> nb;
+        ED::new_model(n, ns, nb, {}, false);
+      } else if (cmd == "el") {
+        string m, op, type; size_t r, c; double v;
+        ss >> m >> op >> type >> r >> c >> v;
+        S.elements[m][op].push_back(matrix_element<double>(r, c, v));
+        S.optype[m][op] = type;
+      } else if (cmd == "param") {
+        string n; double v; ss >> n >> v; S.params[n] = v;
+      } else if (cmd == "instance") {
+        string m, sec; size_t label; ss >> m >> sec >> label;
+        create_ops(S, m);
+        auto v = values_for(S, m);
+        ED::new_model_instance(m, v, sec, label);
+      } else if (cmd == "halfbasis") {
+        int L, N; ss >> L >> N;
+        ED_halfbasis B(L, N);
+        put("halfbasis_L" + to_string(L) + "_N" + to_string(N), "u4", {B.bin.size()},
+            B.bin.data(), B.bin.size());
+      } else if (cmd == "hamiltonian" || cmd == "lanczos") {
+        string m, secs, tag; ss >> m >> secs >> tag;
+        create_ops(S, m);
+        auto mod = models.at(m);
+        if (!mod->is_factorized)
+          throw runtime_error("model " + m + " is not factorized: create an instance with format F first");
+        sector sec(secs);
+        auto v = values_for(S, m);
+        Hamiltonian_Factorized<double> H(mod, v, sec);
+        vector<double> x0 = seeded_start(H.dim);
+        if (cmd == "hamiltonian") {
+          put_d(tag + "_x0", x0);
+          vector<double> y(H.dim, 0.0);
+          H.mult_add(x0, y);
+          put_d(tag + "_Hx0", y);
+          for (auto& t : v) {
+            auto* ob = dynamic_cast<one_body_operator<double>*>(mod->term.at(t.first).get());
+            if (!ob) continue;
+            if (ob->half_operators.count(sec.Nup()))
+              dump_halfop(tag + "_" + t.first + "_up", ob->half_operators.at(sec.Nup()));
+            if (ob->half_operators_dw.count(sec.Ndw()))
+              dump_halfop(tag + "_" + t.first + "_dn", ob->half_operators_dw.at(sec.Ndw()));
+          }
+        } else {
+          vector<double> alpha, beta, energy;
+          size_t niter = 0;
+          vector<double> gs(x0);
+          LanczosEigenvalue(H, gs, alpha, beta, energy, niter, false);
+          put_d(tag + "_alpha", alpha);
+          put_d(tag + "_beta", beta);
+          put_scalar(tag + "_E0", energy[0]);
+          LanczosEigenvector(H, gs, alpha, beta, false);
+          put_d(tag + "_psi", gs);
+        }
+      } else if (cmd == "destroy") {
+        string m, secs, tag; int orb, spin, pm; ss >> m >> secs >> orb >> spin >> pm >> tag;
+        auto mod = models.at(m);
+        sector sec(secs);
+        auto B = mod->provide_factorized_basis(sec);
+        state<double> st(sec, B->dim);
+        st.psi = seeded_start(B->dim);
+        symmetric_orbital a;
+        a.orb = orb; a.spin = spin; a.irrep = 0; a.nambu = 0;
+        vector<double> y;
+        mod->create_or_destroy(pm, a, st, y, 1.0);
+        put_d(tag + "_x", st.psi);
+        put_d(tag + "_y", y);
+      } else if (cmd == "gs") {
+        size_t label; string tag; ss >> label >> tag;
+        auto r = ED::ground_state_solve(label);
+        put_scalar(tag + "_E0", r.first);
+      } else if (cmd == "qmatrix") {
+        size_t label; int spin; string tag; ss >> label >> spin >> tag;
+        ED::Green_function_solve(label);
+        auto q = ED::qmatrix(spin != 0, label);
+        put_d(tag + "_e", q.first);
+        size_t M = q.first.size();
+        size_t L = M ? q.second.size() / M : 0;
+        put(tag + "_v", "c16", {M, L}, q.second.data(), q.second.size());
+      } else if (cmd == "gz" || cmd == "hyb" || cmd == "sigma") {
+        size_t label; int spin; double re, im; string tag;
+        ss >> label >> spin >> re >> im >> tag;
+        cplx z(re, im);
+        ED::Green_function_solve(label);
+        matrix<cplx> G;
+        if (cmd == "gz") G = ED::Green_function(z, spin != 0, label, false);
+        else if (cmd == "hyb") G = ED::hybridization_function(z, spin != 0, label);
+        else G = ED::self_energy(z, spin != 0, label);
+        put_cmat(tag, G);
+      } else if (cmd == "omega") {
+        size_t label; string tag; ss >> label >> tag;
+        ED::Green_function_solve(label);
+        put_scalar(tag, ED::Potthoff_functional(label));
+      } else {
+        throw runtime_error("unknown spec command: " + cmd);
+      }
+    }
+  } catch (std::exception& e) {
+    cerr << "oracle driver error: " << e.what() << endl;
+    return 1;
+  }
+  return 0;
+}

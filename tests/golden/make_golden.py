@@ -1,0 +1,106 @@
+"""Generates the golden fixtures in this folder by running the reference's own
+exact-diagonalization code (compiled by oracle/refbuild into oracle/_ref).
+
+Run from the repository root, in a container that has the reference tree:
+    make -C oracle/refbuild && python tests/golden/make_golden.py
+Each case writes <case>.npz holding the spec it ran and every array the
+reference produced (see oracle/refbuild/ref_driver.cpp for the commands).
+"""
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, HERE)
+from models import hubbard_cluster  # noqa: E402
+
+DRIVER = os.path.join(ROOT, "oracle", "_ref", "qcm_ref_driver")
+DT = {"f8": "<f8", "u4": "<u4", "c16": "<c16"}
+
+
+def run_spec(lines):
+    with tempfile.TemporaryDirectory() as d:
+        spec = os.path.join(d, "spec.txt")
+        with open(spec, "w") as f:
+            f.write("\n".join(lines) + "\n")
+        subprocess.run([DRIVER, spec, d], check=True)
+        out = {}
+        for line in open(os.path.join(d, "manifest.txt")):
+            p = line.split()
+            name, dt, shape = p[0], p[1], tuple(int(s) for s in p[2:])
+            a = np.fromfile(os.path.join(d, name + ".bin"), dtype=DT[dt])
+            out[name] = a.reshape(shape)
+        out["spec"] = np.array("\n".join(lines))
+        return out
+
+
+def model_lines(name, ns, nb, ops):
+    lines = [f"model {name} {ns} {nb}"]
+    for op, (typ, els) in ops.items():
+        for r, c, v in els:
+            lines.append(f"el {name} {op} {typ} {r} {c} {v!r}")
+    return lines
+
+
+def ed_case(tag, nx, ny, params, sector, n_bath=0, af=False, extra=(), gf=True, gz=()):
+    ns, nb, ops = hubbard_cluster(nx, ny, n_bath, af)
+    lines = ["gchar Hamiltonian_format F", "gint seed 0"]
+    lines += model_lines("clus", ns, nb, ops)
+    lines += [f"param {k} {v!r}" for k, v in params.items() if k in ops]
+    lines += [f"instance clus {sector} 1"]
+    lines += list(extra)
+    if gf:
+        lines += ["qmatrix 1 0 qup"]
+        if af:
+            lines += ["qmatrix 1 1 qdn"]
+        for k, z in enumerate(gz):
+            lines += [f"gz 1 0 {z.real!r} {z.imag!r} gz{k}"]
+            if af:
+                lines += [f"gz 1 1 {z.real!r} {z.imag!r} gzdn{k}"]
+            if n_bath:
+                lines += [f"hyb 1 0 {z.real!r} {z.imag!r} hyb{k}",
+                          f"sigma 1 0 {z.real!r} {z.imag!r} sig{k}"]
+        lines += ["omega 1 omega"]
+    lines += ["gs 1 gs"]
+    out = run_spec(lines)
+    np.savez_compressed(os.path.join(HERE, tag + ".npz"), **out)
+    print(tag, sorted(k for k in out if k != "spec"))
+
+
+def main():
+    if not os.path.exists(DRIVER):
+        sys.exit("build the reference oracle first: make -C oracle/refbuild")
+    # Half bases for L = 8, 12, 16 at half filling and one off-half filling.
+    lines = ["halfbasis 8 4", "halfbasis 8 3", "halfbasis 12 6", "halfbasis 12 5", "halfbasis 16 8"]
+    out = run_spec(lines)
+    np.savez_compressed(os.path.join(HERE, "halfbasis.npz"), **out)
+    zs = [0.5j, 0.3 + 0.1j, -1.2 + 0.05j]
+    # 8-site open chain, t=1, U=4, mu=2, half filling (dim 4900).
+    sec = "R0:N8:S0"
+    ed_case("chain8", 8, 1, {"t": 1.0, "U": 4.0, "mu": 2.0}, sec,
+            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz",
+                   f"destroy clus {sec} 3 0 -1 dup", f"destroy clus {sec} 5 1 -1 ddn",
+                   f"destroy clus {sec} 2 0 1 cup", f"destroy clus {sec} 6 1 1 cdn"], gz=zs)
+    # Same chain in an odd sector with Sz = 1 (dims 56 x 35).
+    sec = "R0:N7:S1"
+    ed_case("chain8_n7", 8, 1, {"t": 1.0, "U": 4.0, "mu": 2.0}, sec,
+            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gf=False)
+    # 2x4 cluster with t' and a Neel field M: up and down half-operators differ.
+    sec = "R0:N8:S0"
+    ed_case("ladder2x4_af", 4, 2, {"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0, "M": 0.15}, sec,
+            af=True, extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gz=zs)
+    # 2x2 plaquette + 4 bath orbitals (8 orbitals, dim 4900).
+    params = {"t": 1.0, "U": 4.0, "mu": 2.0}
+    for k in range(4):
+        params[f"eb{k+1}"] = [-1.1, 0.7, 1.3, -0.4][k]
+        params[f"tb{k+1}"] = [0.5, 0.45, 0.6, 0.35][k]
+    ed_case("plaquette_bath4", 2, 2, params, sec, n_bath=4,
+            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gz=zs)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,60 @@
+"""Cluster models used by the golden fixtures and the parity tests.
+
+Each model is a list of named operators given by spin-orbital matrix
+elements in pyqcm's cluster convention: orbitals 0..n_orb-1 are spin up,
+n_orb..2*n_orb-1 spin down; one-body elements (r, c, v) with r <= c are
+completed by their Hermitian conjugate (src_ed/Operators/one_body_operator.hpp:62-71);
+interaction elements (r, c, v) add v*n_r*n_c
+(src_ed/Operators/interaction_operator.hpp:40-52).
+"""
+
+
+def _bonds_2d(nx, ny):
+    """Nearest-neighbour and diagonal bonds of an open nx-by-ny cluster,
+    sites numbered row-major (x fastest)."""
+    nn, diag = [], []
+    for y in range(ny):
+        for x in range(nx):
+            i = x + nx * y
+            if x + 1 < nx:
+                nn.append((i, i + 1))
+            if y + 1 < ny:
+                nn.append((i, i + nx))
+            if x + 1 < nx and y + 1 < ny:
+                diag.append((i, i + 1 + nx))
+            if x - 1 >= 0 and y + 1 < ny:
+                diag.append((i, i - 1 + nx))
+    return nn, diag
+
+
+def hubbard_cluster(nx, ny, n_bath=0, af=False):
+    """Operators of a Hubbard cluster: t (nearest neighbour, amplitude -1),
+    tp (diagonal, amplitude -1), U (on-site), mu (amplitude -1 per orbital of
+    the cluster), optionally the Neel field M (+1 up / -1 down on sublattice A,
+    opposite on B), and bath terms eb{k} (bath energies) and tb{k}
+    (cluster-bath hybridization of bath k with site k % n_sites)."""
+    ns = nx * ny
+    no = ns + n_bath
+    ops = {}
+    nn, diag = _bonds_2d(nx, ny)
+    ops["t"] = ("one-body", [(i, j, -1.0) for i, j in nn] + [(i + no, j + no, -1.0) for i, j in nn])
+    if diag:
+        ops["tp"] = ("one-body", [(i, j, -1.0) for i, j in diag]
+                     + [(i + no, j + no, -1.0) for i, j in diag])
+    ops["U"] = ("interaction", [(i, i + no, 1.0) for i in range(ns)])
+    ops["mu"] = ("one-body", [(i, i, -1.0) for i in range(ns)] + [(i + no, i + no, -1.0) for i in range(ns)])
+    if af:
+        el = []
+        for y in range(ny):
+            for x in range(nx):
+                i = x + nx * y
+                s = 1.0 if (x + y) % 2 == 0 else -1.0
+                el.append((i, i, s))
+                el.append((i + no, i + no, -s))
+        ops["M"] = ("one-body", el)
+    for k in range(n_bath):
+        b = ns + k
+        ops[f"eb{k+1}"] = ("one-body", [(b, b, 1.0), (b + no, b + no, 1.0)])
+        s = k % ns
+        ops[f"tb{k+1}"] = ("one-body", [(s, b, 1.0), (s + no, b + no, 1.0)])
+    return ns, n_bath, ops
