@@ -1,0 +1,270 @@
+"""Benchmark: Lanczos H.psi throughput on the 4x4 Hubbard cluster at half
+filling (16 sites, N=16, Sz=0, sector dimension 165,636,900, FP64 vectors).
+
+A step is one Hamiltonian-vector product y = H x of that sector, the product
+every Lanczos / band-Lanczos iteration performs.  value = algorithmic bytes
+(24 B per basis state: read x, read y, write y) x steps / device time,
+with both vectors (1.33 GB each, larger than L2) resident in HBM.
+e2e = the same metric through the public host API (x copied in from pinned
+host memory, y copied back, every step).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl qcmg|reference]
+
+--impl reference times the CPU oracle's port of the reference's factorized
+product (oracle/qcm_oracle.c) on the host cores with all threads.
+Multi-GPU runs are independent replicas (the product does not shard).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
+
+METRIC = "lanczos_hpsi_gbs"
+UNIT = "GB/s"
+NX, NY = 4, 4
+PARAMS = {"t": 1.0, "U": 8.0, "mu": 4.0}
+SECTOR = "R0:N16:S0"
+BYTES_PER_STATE = 24
+
+
+def workload_config():
+    return {"workload": "4x4 Hubbard cluster, t=1 U=8 mu=4, sector N=16 Sz=0 "
+                        "(dim 165,636,900), y = H x FP64",
+            "dim": 165636900, "bytes_per_step": BYTES_PER_STATE * 165636900,
+            "l2": "inputs larger than L2 (2 x 1.33 GB)", "parallelism": "replicas"}
+
+
+def model_ops():
+    from models import hubbard_cluster
+    return hubbard_cluster(NX, NY)
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic():
+    """Per-launch DRAM bytes of the product kernel from the committed ncu
+    summary, or None."""
+    p = os.path.join(ROOT, "profiles", "matvec_4x4_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        if line.startswith("dram_bytes_per_launch_full:"):
+            return float(line.split(":")[1])
+    return None
+
+
+class ClockSampler:
+    """Samples nvidia-smi SM clocks and throttle reasons while running."""
+
+    def __init__(self, index=0):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(self.rows)}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def cpu_port_timing(steps, threads):
+    """Times the oracle's port of the reference's factorized product on the
+    host (all `threads`), on the same sector; returns (GB/s, seconds/step)."""
+    import numpy as np
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import qcm_oracle as qo
+    ns, nb, ops = model_ops()
+    up, dn, pr = qo.combine_terms(ops, PARAMS, ns)
+    S = qo.Sector(ns, 8, 8, up, dn, pr)
+    x = np.random.default_rng(1).standard_normal(S.dim)
+    x /= np.linalg.norm(x)
+    y = np.zeros(S.dim)
+    S.mult_add(x, y, nthreads=threads)  # warm-up (page faults)
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        S.mult_add(x, y, nthreads=threads)
+    dt = (time.perf_counter() - t0) / steps
+    return BYTES_PER_STATE * S.dim / dt / 1e9, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    steps = max(1, args.steps)
+    gbs, dt = cpu_port_timing(steps, threads)
+    sample = f"{steps} full products y += H x on the 4x4 N=16 Sz=0 sector, {threads} threads"
+    line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(),
+            "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import pyqcm_gb300 as pg
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    pg._lib.check(pg.lib().qcmg_set_device(local))
+    ns, nb, ops = model_ops()
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, PARAMS, SECTOR)
+    D = H.dim
+    stream = torch.cuda.current_stream()
+    H.set_stream(stream.cuda_stream)
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
+    x /= torch.linalg.vector_norm(x)
+    y = torch.zeros(D, dtype=torch.float64, device="cuda")
+    for _ in range(args.warmup):
+        H.matvec_device(x.data_ptr(), y.data_ptr(), asynchronous=True)
+    torch.cuda.synchronize()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        t_all0 = torch.cuda.Event(enable_timing=True)
+        t_all1 = torch.cuda.Event(enable_timing=True)
+        t_all0.record(stream)
+        for k in range(args.steps):
+            starts[k].record(stream)
+            H.matvec_device(x.data_ptr(), y.data_ptr(), asynchronous=True)
+            ends[k].record(stream)
+        t_all1.record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    total_ms = t_all0.elapsed_time(t_all1)
+    per_launch = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    if world > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    bytes_step = BYTES_PER_STATE * D
+    value = bytes_step * args.steps * world / (total_ms * 1e-3) / 1e9
+    avg_launch_ms = sum(per_launch) / len(per_launch)
+    achieved = bytes_step / (avg_launch_ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+
+    # e2e through the public host API: pinned host x in, y out, every step.
+    xh = torch.empty(D, dtype=torch.float64, pin_memory=True)
+    xh.copy_(x.cpu())
+    xn = xh.numpy()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(2, min(args.steps, 5))
+    H.set_stream(0)
+    H.matvec(xn)  # warm-up of the staging buffers
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        yh = H.matvec(xn)
+    e2e_s = (time.perf_counter() - t0) / e2e_steps
+    e2e_val = bytes_step * world / e2e_s / 1e9
+    del ev0, yh
+
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": UNIT,
+                         "frac": achieved / peak, "traffic": profile_traffic(),
+                         "peak_kind": peak_kind, "kernel": "k_matvec_f64"},
+            "clocks": clocks.summary(),
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * D,
+                    "d2h_bytes_per_step": 8 * D},
+            "gpu_launches": args.steps}
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        gbs, dt = cpu_port_timing(1, threads)
+        line["cpu_baseline"] = {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"1 full product y += H x on the same sector, "
+                                          f"{threads} threads ({dt:.2f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="qcmg", choices=["qcmg", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,170 @@
+/* qcmg.h -- C ABI of the GB300 (sm_103a) engine for pyqcm's exact
+ * diagonalization hot path: the factorized Hubbard Hamiltonian-vector product
+ * inside Lanczos and band Lanczos, the Lehmann (Q-matrix) Green function, and
+ * the CPT/VCA/CDMFT k x omega lattice integrals over it.
+ *
+ * Plain C types only: pointers, sizes, doubles.  Every function returns 0 on
+ * success or a negative QCMG_ERR_* code; qcmg_last_error() then holds a
+ * message for the calling thread.  Handles are independent: two threads may
+ * use two handles concurrently; one handle must not be used by two threads
+ * at once.  All arrays are caller-owned.  Unless a flag says otherwise,
+ * vector arguments are HOST pointers and the call copies them to and from the
+ * device; with QCMG_DEVICE_PTRS they are device pointers on the handle's GPU.
+ *
+ * Conventions shared with the reference (pyqcm, src_ed/):
+ *  - orbitals 0..L-1 are spin up, L..2L-1 spin down; a one-body element
+ *    (r, c, v) is v c^dagger_r c_c and must be given for both (r,c) and (c,r);
+ *  - half basis of a spin = increasing L-bit integers with popcount N
+ *    (src_ed/ED_basis.cpp:115-135); factorized index
+ *    I = i_up + dim_up * i_dn (src_ed/ED_basis.cpp:142-165);
+ *  - a hop r <- c carries the sign (-1)^(occupied orbitals strictly between)
+ *    (src_ed/binary_state.hpp:42-49).
+ */
+#ifndef QCMG_H
+#define QCMG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QCMG_OK 0
+#define QCMG_ERR_ARG -1      /* invalid argument (size, index, null pointer) */
+#define QCMG_ERR_CUDA -2     /* CUDA runtime or library failure */
+#define QCMG_ERR_NOMEM -3    /* device allocation failed */
+#define QCMG_ERR_NOCONV -4   /* iteration limit reached before convergence */
+#define QCMG_ERR_DEVICE -5   /* no usable GPU */
+#define QCMG_ERR_NUMERIC -6  /* non-finite value or breakdown detected */
+
+#define QCMG_DEVICE_PTRS 1u  /* vector arguments are device pointers */
+#define QCMG_ACCUMULATE 2u   /* y += H x (otherwise y = H x) */
+#define QCMG_ASYNC 4u        /* with QCMG_DEVICE_PTRS: return without waiting for the GPU */
+
+typedef struct qcmg_hamiltonian qcmg_hamiltonian;
+
+/* Version string of the library. */
+const char* qcmg_version(void);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated,
+ * truncated to n bytes).  Returns the full message length. */
+size_t qcmg_last_error(char* buf, size_t n);
+
+/* Selects the GPU used by handles created afterwards on this thread. */
+int qcmg_set_device(int device);
+
+/* Half basis of L orbitals with N electrons, built on the GPU by unranking
+ * the combinatorial number system.  Writes at most cap states into out and
+ * the dimension C(L,N) into *dim.
+ * Replaces ED_halfbasis::ED_halfbasis (src_ed/ED_basis.cpp:115-125). */
+int qcmg_halfbasis(int L, int N, uint32_t* out, size_t cap, size_t* dim);
+
+/* Ranks of n half-states (popcount N) computed on the GPU; a state that is
+ * not in the basis gets rank dim.
+ * Replaces ED_halfbasis::index (src_ed/ED_basis.cpp:130-135). */
+int qcmg_halfbasis_rank(int L, int N, const uint32_t* states, size_t n, uint32_t* ranks);
+
+/* Factorized Hamiltonian of the sector (N_up, N_dn) on L orbitals:
+ *   H = T_dn (x) 1 + 1 (x) T_up + sum_pairs v n_r n_c
+ * hop_{up,dn}: n_hop one-body elements (r, c, v) of each spin, with r, c in
+ *   0..L-1, the coefficients of the value map already applied and both
+ *   triangles given (r == c adds v n_r);
+ * pairs: n_pair density-density elements (r, c, v) on spin-orbitals
+ *   0..2L-1, adding v n_r n_c.
+ * The half-operators are built on the GPU from these elements.
+ * Replaces Hamiltonian_Factorized::Hamiltonian_Factorized and its
+ * HS_ops_map (src_ed/Hamiltonian/Hamiltonian_Factorized.hpp:31-87), the
+ * HS_half_operator construction (src_ed/Operators/HS_half_operator.hpp:21-45)
+ * and the HS_interaction_operator table
+ * (src_ed/Operators/HS_interaction_operator.hpp:32-54). */
+int qcmg_hamiltonian_create(int L, int n_up, int n_dn,
+                            int n_hop_up, const int32_t* up_r, const int32_t* up_c,
+                            const double* up_v,
+                            int n_hop_dn, const int32_t* dn_r, const int32_t* dn_c,
+                            const double* dn_v,
+                            int n_pair, const int32_t* pair_r, const int32_t* pair_c,
+                            const double* pair_v,
+                            qcmg_hamiltonian** out);
+
+int qcmg_hamiltonian_destroy(qcmg_hamiltonian* H);
+
+/* Makes the handle launch its work on `stream` (a cudaStream_t of the
+ * handle's device; NULL restores the handle's own stream).  No counterpart
+ * in the reference, whose products run on the calling CPU thread. */
+int qcmg_hamiltonian_set_stream(qcmg_hamiltonian* H, void* stream);
+
+/* Sector dimensions: dim_up, dim_dn and dim = dim_up * dim_dn. */
+int qcmg_hamiltonian_dims(const qcmg_hamiltonian* H, size_t* dim_up, size_t* dim_dn,
+                          size_t* dim);
+
+/* Exports the half-operator of one spin (0 up, 1 down) as CSR rows indexed
+ * by the input state: rowptr[dim_s+1], col[nnz], val[nnz], diag[dim_s].
+ * Call with rowptr == NULL to get *nnz only.  For checking against the
+ * reference's HS_half_operator tables. */
+int qcmg_hamiltonian_halfop(const qcmg_hamiltonian* H, int spin, size_t* nnz, uint32_t* rowptr,
+                            uint32_t* col, double* val, double* diag);
+
+/* y = H x, or y += H x with QCMG_ACCUMULATE.  x and y have length dim.
+ * Replaces Hamiltonian_Factorized::mult_add
+ * (src_ed/Hamiltonian/Hamiltonian_Factorized.hpp:50-58) with
+ * HS_factorized_operator::multiply_add (HS_factorized_operator.hpp:57-84)
+ * and HS_interaction_operator::multiply_add (HS_interaction_operator.hpp:62-70). */
+int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags);
+
+/* Seeded start vector of the reference: std::default_random_engine(seed)
+ * drawing std::normal_distribution(0,1), normalized.
+ * Replaces random() (src_util/vector_num.cpp:114-119). */
+int qcmg_seeded_vector(size_t dim, unsigned seed, double* out);
+
+/* Lanczos ground state.  x0 (length dim, normalized; NULL = seeded start
+ * with `seed`) starts the three-term recurrence of the reference
+ * (no reorthogonalization when reorth == 0); iteration stops when the Ritz
+ * residual |s_last * beta| < tol or after max_iter steps.  With reorth > 0 the
+ * Lanczos basis is kept on the device and every new vector is
+ * reorthogonalized (classical Gram-Schmidt, twice) against all previous ones;
+ * at most `reorth` vectors are kept.
+ * Outputs: *E0; psi (length dim, may be NULL: then no second pass);
+ * *niter; alpha, beta (capacity `cap`, may be NULL).
+ * Replaces LanczosEigenvalue + LanczosEigenvector
+ * (src_ed/Hamiltonian/Lanczos.hpp:41-143) as called from
+ * Hamiltonian::states (src_ed/Hamiltonian/Hamiltonian_base.hpp:114-221). */
+int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned seed, double tol,
+                              int max_iter, int reorth, double* E0, double* psi, int* niter,
+                              double* alpha, double* beta, int cap);
+
+/* Band Lanczos from p start vectors phi (p x dim, row-major: vector k at
+ * phi + k*dim).  M_target is the requested number of steps (the reference
+ * uses 14 p ln(dim), capped at max_iter); deflation below acc_deflation;
+ * stops when the lowest eigenvalue of the projected matrix moves by less
+ * than acc_band between checks.
+ * Outputs: *M (number of poles), evals[M] and Q (p x M, row-major) =
+ * P U restricted to the first p Lanczos vectors; caller capacity `cap` >= M.
+ * Replaces bandLanczos + Hamiltonian::build_Q_matrix
+ * (src_ed/Hamiltonian/Lanczos.hpp:214-395, Hamiltonian_base.hpp:229-254). */
+int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_target, int max_iter,
+                      double acc_deflation, double acc_band, int* M, double* evals, double* Q,
+                      int cap);
+
+/* c_orb (pm = -1) or c^dagger_orb (pm = +1) applied to x of sector
+ * (n_up, n_dn) on L orbitals; orb >= L is a down orbital.  y (target sector,
+ * length dim_up' * dim_dn') receives y (+)= z * c x.
+ * Replaces model::create_or_destroy, factorized branch
+ * (src_ed/model.cpp:155-180) with Destroy (src_ed/ED_basis.cpp:79-110). */
+int qcmg_apply_c(int L, int orb, int pm, int n_up, int n_dn, const double* x, double* y,
+                 double z, unsigned flags);
+
+/* Lehmann Green function G(z_w) = sum_i v_i v_i^dagger / (z_w - e_i) for nz
+ * frequencies, batched on the GPU.  e[M]; v: complex L x M (interleaved
+ * re,im, column-major: element (a,i) at 2*(a + L*i)); z: nz complex
+ * (interleaved); G: nz blocks of L x L complex, column-major, in the
+ * reference's orientation G(b,a) = sum_i v_ai u_i conj(v_bi).
+ * Replaces Q_matrix::Green_function + VDVH_naive
+ * (src_ed/Q_matrix.hpp:133-151, src_util/VDVH_kernel.cpp:28-48). */
+int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, const double* z,
+                        double* G);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

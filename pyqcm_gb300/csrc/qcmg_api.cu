@@ -1,0 +1,411 @@
+// C ABI entry points (declared in include/qcmg.h): argument checking, error
+// reporting, host<->device staging, and the handle lifetime.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "qcmg.h"
+#include "qcmg_internal.h"
+#include "qcmg_krylov.h"
+
+namespace qcmg {
+
+static thread_local std::string g_error;
+static thread_local int g_device = 0;
+
+void set_error(const std::string& msg) { g_error = msg; }
+void clear_error() { g_error.clear(); }
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    clear_error();
+    f();
+    return QCMG_OK;
+  } catch (const Error& e) {
+    set_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return QCMG_ERR_NOMEM;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return QCMG_ERR_CUDA;
+  }
+}
+
+static void use_device() {
+  int n = 0;
+  cudaError_t e = cudaGetDeviceCount(&n);
+  if (e != cudaSuccess || n == 0)
+    throw Error(QCMG_ERR_DEVICE, std::string("no usable CUDA device: ") + cudaGetErrorString(e));
+  if (g_device >= n) throw Error(QCMG_ERR_DEVICE, "device index out of range");
+  QCMG_CUDA(cudaSetDevice(g_device));
+  ensure_device_tables(g_device);
+}
+
+static unsigned classify_onsite(const std::vector<double>& W, int L, double* U, uint32_t* mask) {
+  // Diagonal with a single nonzero value -> U * popcount(u & d & mask).
+  double u = 0.0;
+  uint32_t m = 0;
+  for (int r = 0; r < L; ++r)
+    for (int c = 0; c < L; ++c) {
+      double w = W[(size_t)r * L + c];
+      if (w == 0.0) continue;
+      if (r != c) return QCMG_INTER_GENERAL;
+      if (u == 0.0) u = w;
+      if (w != u) return QCMG_INTER_GENERAL;
+      m |= 1u << r;
+    }
+  if (u == 0.0) return QCMG_INTER_NONE;
+  *U = u;
+  *mask = m;
+  return QCMG_INTER_ONSITE;
+}
+
+}  // namespace qcmg
+
+using namespace qcmg;
+
+// ---------------------------------------------------------------------------
+// Same-spin density-density pairs are diagonal in one half basis: fold them
+// into that spin's diagonal.  Cross-spin pairs W[r_up][c_dn] are evaluated in
+// the product (on-site fast path) or tabulated per down state.
+
+__global__ void k_pair_diag(uint32_t dim, const uint32_t* __restrict__ bin, int r, int c, double v,
+                            double* __restrict__ diag) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < dim; i += gridDim.x * blockDim.x) {
+    uint32_t b = bin[i];
+    if (((b >> r) & 1u) && ((b >> c) & 1u)) diag[i] += v;
+  }
+}
+
+__global__ void k_cross_table(uint32_t dd, int L, const uint32_t* __restrict__ bin_dn,
+                              const double* __restrict__ W, double* __restrict__ wdn) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < dd; i += gridDim.x * blockDim.x) {
+    uint32_t d = bin_dn[i];
+    for (int r = 0; r < L; ++r) {
+      double s = 0.0;
+      for (int c = 0; c < L; ++c)
+        if ((d >> c) & 1u) s += W[(size_t)r * L + c];
+      wdn[(size_t)i * L + r] = s;
+    }
+  }
+}
+
+extern "C" {
+
+const char* qcmg_version(void) { return "qcmg 0.1 (sm_103a)"; }
+
+size_t qcmg_last_error(char* buf, size_t n) {
+  if (buf && n) {
+    size_t k = std::min(n - 1, g_error.size());
+    std::memcpy(buf, g_error.data(), k);
+    buf[k] = 0;
+  }
+  return g_error.size();
+}
+
+int qcmg_set_device(int device) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(device >= 0, "negative device index");
+    g_device = device;
+    use_device();
+  });
+}
+
+int qcmg_halfbasis(int L, int N, uint32_t* out, size_t cap, size_t* dim) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(L >= 1 && L <= kMaxOrbitals, "L must be in 1..32");
+    QCMG_CHECK_ARG(dim != nullptr, "dim is NULL");
+    uint64_t d = (N < 0 || N > L) ? 0 : binomial(L, N);
+    *dim = (size_t)d;
+    if (!d || !out || !cap) return;
+    QCMG_CHECK_ARG(d < (1ull << 31), "half basis too large");
+    use_device();
+    DevBuf<uint32_t> buf;
+    buf.alloc(d);
+    launch_halfbasis(L, N, (uint32_t)d, buf.p, 0);
+    QCMG_CUDA(cudaMemcpy(out, buf.p, std::min<size_t>(cap, d) * 4, cudaMemcpyDeviceToHost));
+  });
+}
+
+int qcmg_halfbasis_rank(int L, int N, const uint32_t* states, size_t n, uint32_t* ranks) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(L >= 1 && L <= kMaxOrbitals, "L must be in 1..32");
+    QCMG_CHECK_ARG(N >= 0 && N <= L, "N out of range");
+    if (!n) return;
+    QCMG_CHECK_ARG(states && ranks, "NULL array");
+    use_device();
+    uint32_t d = (uint32_t)binomial(L, N);
+    // States with the wrong popcount are not in the basis: mark them first.
+    std::vector<uint32_t> st(states, states + n);
+    DevBuf<uint32_t> ds, dr;
+    ds.upload(st.data(), n, 0);
+    dr.alloc(n);
+    launch_rank(L, ds.p, n, d, dr.p, 0);
+    QCMG_CUDA(cudaMemcpy(ranks, dr.p, n * 4, cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i)
+      if (__builtin_popcount(st[i]) != N) ranks[i] = d;
+  });
+}
+
+int qcmg_hamiltonian_create(int L, int n_up, int n_dn, int n_hop_up, const int32_t* up_r,
+                            const int32_t* up_c, const double* up_v, int n_hop_dn,
+                            const int32_t* dn_r, const int32_t* dn_c, const double* dn_v,
+                            int n_pair, const int32_t* pair_r, const int32_t* pair_c,
+                            const double* pair_v, qcmg_hamiltonian** out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(out != nullptr, "out is NULL");
+    *out = nullptr;
+    QCMG_CHECK_ARG(L >= 1 && L <= kMaxOrbitals, "L must be in 1..32");
+    QCMG_CHECK_ARG(n_up >= 0 && n_up <= L && n_dn >= 0 && n_dn <= L, "electron count out of range");
+    QCMG_CHECK_ARG(n_hop_up >= 0 && n_hop_dn >= 0 && n_pair >= 0, "negative element count");
+    QCMG_CHECK_ARG((n_hop_up == 0 || (up_r && up_c && up_v)) &&
+                       (n_hop_dn == 0 || (dn_r && dn_c && dn_v)) &&
+                       (n_pair == 0 || (pair_r && pair_c && pair_v)),
+                   "NULL element array");
+    for (int k = 0; k < n_hop_up + n_hop_dn + n_pair; ++k) {
+      double v = k < n_hop_up ? up_v[k]
+                 : k < n_hop_up + n_hop_dn ? dn_v[k - n_hop_up]
+                                           : pair_v[k - n_hop_up - n_hop_dn];
+      QCMG_CHECK_ARG(std::isfinite(v), "non-finite matrix element");
+    }
+    use_device();
+    auto* H = new qcmg_hamiltonian();
+    try {
+      H->device = g_device;
+      H->L = L;
+      H->nup = n_up;
+      H->ndn = n_dn;
+      QCMG_CUDA(cudaStreamCreateWithFlags(&H->own_stream, cudaStreamNonBlocking));
+      H->stream = H->own_stream;
+      std::vector<HopElement> eu, ed;
+      for (int k = 0; k < n_hop_up; ++k) eu.push_back({up_r[k], up_c[k], up_v[k]});
+      for (int k = 0; k < n_hop_dn; ++k) ed.push_back({dn_r[k], dn_c[k], dn_v[k]});
+      build_halfop(H->up, L, n_up, eu, H->stream);
+      build_halfop(H->dn, L, n_dn, ed, H->stream);
+      H->du = H->up.dim;
+      H->dd = H->dn.dim;
+      H->dim = (size_t)H->du * H->dd;
+      std::vector<double> W((size_t)L * L, 0.0);
+      for (int k = 0; k < n_pair; ++k) {
+        int r = pair_r[k], c = pair_c[k];
+        double v = pair_v[k];
+        QCMG_CHECK_ARG(r >= 0 && r < 2 * L && c >= 0 && c < 2 * L, "pair orbital out of range");
+        if (v == 0.0) continue;
+        bool ru = r < L, cu = c < L;
+        if (ru && cu) {
+          if (H->du)
+            k_pair_diag<<<(H->du + 255) / 256, 256, 0, H->stream>>>(H->du, H->up.bin.p, r, c, v,
+                                                                    H->up.diag.p);
+        } else if (!ru && !cu) {
+          if (H->dd)
+            k_pair_diag<<<(H->dd + 255) / 256, 256, 0, H->stream>>>(H->dd, H->dn.bin.p, r - L,
+                                                                    c - L, v, H->dn.diag.p);
+        } else if (ru) {
+          W[(size_t)r * L + (c - L)] += v;
+        } else {
+          W[(size_t)c * L + (r - L)] += v;
+        }
+        QCMG_CUDA(cudaGetLastError());
+      }
+      uint32_t mask = 0;
+      H->inter_kind = (int)classify_onsite(W, L, &H->U, &mask);
+      H->max_inter_abs = 0.0;
+      for (int r = 0; r < L; ++r) {
+        double s = 0.0;
+        for (int c = 0; c < L; ++c) s += std::fabs(W[(size_t)r * L + c]);
+        H->max_inter_abs += s;
+      }
+      if (H->inter_kind == QCMG_INTER_ONSITE && mask != (L >= 32 ? 0xffffffffu : (1u << L) - 1u)) {
+        // masked on-site term (e.g. no U on bath orbitals): tabulate instead
+        H->inter_kind = QCMG_INTER_GENERAL;
+      }
+      if (H->inter_kind == QCMG_INTER_GENERAL && H->dd) {
+        DevBuf<double> dW;
+        dW.upload(W.data(), W.size(), H->stream);
+        H->wdn.alloc((size_t)H->dd * L);
+        k_cross_table<<<(H->dd + 127) / 128, 128, 0, H->stream>>>(H->dd, L, H->dn.bin.p, dW.p,
+                                                                  H->wdn.p);
+        QCMG_CUDA(cudaGetLastError());
+        QCMG_CUDA(cudaStreamSynchronize(H->stream));
+      }
+      QCMG_CUDA(cudaStreamSynchronize(H->stream));
+    } catch (...) {
+      if (H->own_stream) cudaStreamDestroy(H->own_stream);
+      delete H;
+      throw;
+    }
+    *out = H;
+  });
+}
+
+int qcmg_hamiltonian_destroy(qcmg_hamiltonian* H) {
+  return guarded([&] {
+    if (!H) return;
+    cudaSetDevice(H->device);
+    if (H->stream) cudaStreamSynchronize(H->stream);
+    if (H->own_stream) cudaStreamDestroy(H->own_stream);
+    delete H;
+  });
+}
+
+int qcmg_hamiltonian_set_stream(qcmg_hamiltonian* H, void* stream) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr, "NULL handle");
+    std::lock_guard<std::mutex> lock(H->mu);
+    H->stream = stream ? (cudaStream_t)stream : H->own_stream;
+  });
+}
+
+int qcmg_hamiltonian_dims(const qcmg_hamiltonian* H, size_t* du, size_t* dd, size_t* dim) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr, "NULL handle");
+    if (du) *du = H->du;
+    if (dd) *dd = H->dd;
+    if (dim) *dim = H->dim;
+  });
+}
+
+int qcmg_hamiltonian_halfop(const qcmg_hamiltonian* H, int spin, size_t* nnz, uint32_t* rowptr,
+                            uint32_t* col, double* val, double* diag) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && nnz != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(spin == 0 || spin == 1, "spin must be 0 or 1");
+    const HalfOp& op = spin ? H->dn : H->up;
+    *nnz = op.nnz;
+    if (!rowptr) return;
+    QCMG_CUDA(cudaSetDevice(H->device));
+    QCMG_CUDA(cudaMemcpy(rowptr, op.rowptr.p, (op.dim + 1) * 4, cudaMemcpyDeviceToHost));
+    if (op.nnz && col) QCMG_CUDA(cudaMemcpy(col, op.col.p, op.nnz * 4, cudaMemcpyDeviceToHost));
+    if (op.nnz && val) QCMG_CUDA(cudaMemcpy(val, op.val.p, op.nnz * 8, cudaMemcpyDeviceToHost));
+    if (op.dim && diag) QCMG_CUDA(cudaMemcpy(diag, op.diag.p, op.dim * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
+int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && x != nullptr && y != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(x != y, "x and y must not alias");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    const bool acc = (flags & QCMG_ACCUMULATE) != 0;
+    const size_t n = H->dim;
+    if (flags & QCMG_DEVICE_PTRS) {
+      matvec(H, x, y, acc);
+      if (!(flags & QCMG_ASYNC)) QCMG_CUDA(cudaStreamSynchronize(H->stream));
+      return;
+    }
+    H->xbuf.alloc(n);
+    H->ybuf.alloc(n);
+    QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
+    if (acc) QCMG_CUDA(cudaMemcpyAsync(H->ybuf.p, y, n * 8, cudaMemcpyHostToDevice, H->stream));
+    matvec(H, H->xbuf.p, H->ybuf.p, acc);
+    QCMG_CUDA(cudaMemcpyAsync(y, H->ybuf.p, n * 8, cudaMemcpyDeviceToHost, H->stream));
+    QCMG_CUDA(cudaStreamSynchronize(H->stream));
+  });
+}
+
+int qcmg_seeded_vector(size_t dim, unsigned seed, double* out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(out != nullptr || dim == 0, "NULL output");
+    seeded_vector(dim, seed, out);
+  });
+}
+
+int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned seed, double tol,
+                              int max_iter, int reorth, double* E0, double* psi, int* niter,
+                              double* alpha, double* beta, int cap) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && E0 != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(tol > 0.0 && max_iter > 0, "tol and max_iter must be positive");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    LanczosResult r = lanczos_ground_state(H, x0, seed, tol, max_iter, reorth, psi);
+    *E0 = r.energy;
+    if (niter) *niter = r.niter;
+    for (int k = 0; k < std::min<int>(cap, r.niter); ++k) {
+      if (alpha) alpha[k] = r.alpha[k];
+      if (beta) beta[k] = r.beta[k];
+    }
+  });
+}
+
+int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_target, int max_iter,
+                      double acc_deflation, double acc_band, int* M, double* evals, double* Q,
+                      int cap) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && phi != nullptr && M != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(p > 0 && M_target > 1 && max_iter > 0, "invalid band Lanczos sizes");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    *M = 0;
+    if (H->dim == 0) return;
+    BandResult r = band_lanczos(H, p, phi, M_target, max_iter, acc_deflation, acc_band);
+    *M = r.M;
+    QCMG_CHECK_ARG(r.M <= cap, "band Lanczos output capacity too small");
+    if (evals) std::copy(r.evals.begin(), r.evals.end(), evals);
+    if (Q) std::copy(r.Q.begin(), r.Q.end(), Q);
+  });
+}
+
+int qcmg_apply_c(int L, int orb, int pm, int n_up, int n_dn, const double* x, double* y, double z,
+                 unsigned flags) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(L >= 1 && L <= kMaxOrbitals, "L must be in 1..32");
+    QCMG_CHECK_ARG(orb >= 0 && orb < 2 * L, "orbital out of range");
+    QCMG_CHECK_ARG(pm == 1 || pm == -1, "pm must be +1 or -1");
+    QCMG_CHECK_ARG(n_up >= 0 && n_up <= L && n_dn >= 0 && n_dn <= L, "electron count out of range");
+    QCMG_CHECK_ARG(x && y, "NULL vector");
+    const int spin = orb >= L ? 1 : 0, o = spin ? orb - L : orb;
+    const int nup2 = n_up + (spin ? 0 : pm), ndn2 = n_dn + (spin ? pm : 0);
+    const size_t n1 = (size_t)binomial(L, n_up) * binomial(L, n_dn);
+    const size_t n2 = (nup2 < 0 || ndn2 < 0 || nup2 > L || ndn2 > L)
+                          ? 0
+                          : (size_t)binomial(L, nup2) * binomial(L, ndn2);
+    if (n2 == 0) return;
+    use_device();
+    const bool acc = (flags & QCMG_ACCUMULATE) != 0;
+    if (flags & QCMG_DEVICE_PTRS) {
+      launch_apply_c(L, o, spin, pm, n_up, n_dn, x, y, z, acc, 0);
+      QCMG_CUDA(cudaStreamSynchronize(0));
+      return;
+    }
+    DevBuf<double> dx, dy;
+    dx.upload(x, n1, 0);
+    if (acc)
+      dy.upload(y, n2, 0);
+    else
+      dy.alloc(n2);
+    launch_apply_c(L, o, spin, pm, n_up, n_dn, dx.p, dy.p, z, acc, 0);
+    QCMG_CUDA(cudaMemcpy(y, dy.p, n2 * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
+int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, const double* z,
+                        double* G) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(L > 0 && M >= 0 && nz >= 0, "invalid sizes");
+    QCMG_CHECK_ARG(z && G && (M == 0 || (e && v)), "NULL argument");
+    if (nz == 0) return;
+    if (M == 0) {
+      std::fill(G, G + (size_t)2 * L * L * nz, 0.0);
+      return;
+    }
+    use_device();
+    DevBuf<double> de, dv, dz, dG;
+    de.upload(e, M, 0);
+    dv.upload(v, (size_t)2 * L * M, 0);
+    dz.upload(z, (size_t)2 * nz, 0);
+    dG.alloc((size_t)2 * L * L * nz);
+    green_function_batch(L, M, de.p, dv.p, nz, dz.p, dG.p, 0);
+    QCMG_CUDA(cudaMemcpy(G, dG.p, (size_t)2 * L * L * nz * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
+}  // extern "C"

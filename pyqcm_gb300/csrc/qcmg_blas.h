@@ -1,0 +1,32 @@
+// Vector kernels of the Krylov solvers (host launch wrappers).
+#pragma once
+
+#include "qcmg_internal.h"
+
+namespace qcmg {
+
+constexpr int kRedThreads = 256;  // threads per reduction block
+constexpr int kRedBlocks = 1024;  // fixed partial count of a reduction
+
+// Deterministic dot products and norms: fixed grid, fixed-order final sum.
+// Holds its own scratch: one Reducer per handle (not shared across threads).
+struct Reducer {
+  DevBuf<double> part;
+  DevBuf<double> out;
+  double* host = nullptr;  // pinned
+  Reducer() = default;
+  Reducer(const Reducer&) = delete;
+  ~Reducer();
+  void init();
+  double dot(const double* x, const double* y, size_t n, cudaStream_t s);
+  // r -= alpha q; returns |r|^2.
+  double axpy_norm2(double* r, const double* q, double alpha, size_t n, cudaStream_t s);
+};
+
+void axpy(double* y, const double* x, double a, size_t n, cudaStream_t s);
+void scale2(double* r, double s1, double* q, double s2, size_t n, cudaStream_t s);
+void scale(double* x, double a, size_t n, cudaStream_t s);
+void replay_step(double* r, double* q, double* gs, double alpha, double beta, double c, size_t n,
+                 cudaStream_t s);
+
+}  // namespace qcmg

@@ -1,0 +1,126 @@
+// Internal declarations of the qcmg engine (not part of the C ABI).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "qcmg.h"
+
+namespace qcmg {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+void set_error(const std::string& msg);
+void clear_error();
+
+#define QCMG_CUDA(call)                                                                 \
+  do {                                                                                  \
+    cudaError_t err_ = (call);                                                          \
+    if (err_ != cudaSuccess)                                                            \
+      throw ::qcmg::Error(err_ == cudaErrorMemoryAllocation ? QCMG_ERR_NOMEM : QCMG_ERR_CUDA, \
+                          std::string(#call) + ": " + cudaGetErrorString(err_));        \
+  } while (0)
+
+#define QCMG_CHECK_ARG(cond, msg) \
+  do {                            \
+    if (!(cond)) throw ::qcmg::Error(QCMG_ERR_ARG, msg); \
+  } while (0)
+
+// Owning device buffer.
+template <class T>
+struct DevBuf {
+  T* p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  void alloc(size_t count) {
+    if (count <= n && p) return;
+    release();
+    size_t bytes = (count ? count : 1) * sizeof(T);
+    QCMG_CUDA(cudaMalloc(&p, bytes));
+    n = count;
+  }
+  void upload(const T* h, size_t count, cudaStream_t s) {
+    alloc(count);
+    if (count) QCMG_CUDA(cudaMemcpyAsync(p, h, count * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+};
+
+// Largest orbital count a half-state can hold (uint32 bit masks).
+constexpr int kMaxOrbitals = 32;
+
+// Per-device one-time set-up (binomial table in constant memory).
+void ensure_device_tables(int device);
+
+// Half-operator of one spin on the device, CSR rows indexed by the input
+// state: row I lists (J, value) for every hop I -> J, plus the diagonal.
+struct HalfOp {
+  int L = 0, N = 0;
+  uint32_t dim = 0;
+  size_t nnz = 0;
+  DevBuf<uint32_t> bin;     // basis states, increasing
+  DevBuf<uint32_t> rowptr;  // dim + 1
+  DevBuf<uint32_t> col;     // nnz
+  DevBuf<double> val;       // nnz
+  DevBuf<double> diag;      // dim
+  double max_row_abs = 0.0; // max_I sum_J |val| (for fixed-point headroom)
+  double max_diag_abs = 0.0;
+};
+
+struct HopElement {
+  int32_t r, c;
+  double v;
+};
+
+// Device kernels launched from host code (defined in .cu files).
+void launch_halfbasis(int L, int N, uint32_t dim, uint32_t* out, cudaStream_t s);
+void launch_rank(int L, const uint32_t* states, size_t n, uint32_t dim, uint32_t* ranks,
+                 cudaStream_t s);
+void build_halfop(HalfOp& op, int L, int N, const std::vector<HopElement>& el, cudaStream_t s);
+
+uint64_t binomial(int n, int k);
+
+}  // namespace qcmg
+
+// Interaction diagonal kinds.
+enum { QCMG_INTER_NONE = 0, QCMG_INTER_ONSITE = 1, QCMG_INTER_GENERAL = 2 };
+
+struct qcmg_hamiltonian {
+  int device = 0;
+  int L = 0, nup = 0, ndn = 0;
+  uint32_t du = 0, dd = 0;
+  size_t dim = 0;
+  qcmg::HalfOp up, dn;
+  int inter_kind = QCMG_INTER_NONE;
+  double U = 0.0;                 // uniform on-site value (QCMG_INTER_ONSITE)
+  qcmg::DevBuf<double> wdn;       // dd x L cross terms (QCMG_INTER_GENERAL)
+  double max_inter_abs = 0.0;
+  cudaStream_t stream = nullptr;      // stream the handle launches on
+  cudaStream_t own_stream = nullptr;  // created with the handle
+  // staging for host-pointer calls
+  qcmg::DevBuf<double> xbuf, ybuf;
+  // deterministic reduction scratch
+  qcmg::DevBuf<double> partials;
+  qcmg::DevBuf<double> scalars;
+  std::mutex mu;  // serializes calls on one handle
+};
+
+namespace qcmg {
+// Matrix-free factorized product y (+)= H x on the handle's stream.
+void matvec(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
+}  // namespace qcmg

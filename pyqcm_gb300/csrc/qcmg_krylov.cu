@@ -1,0 +1,415 @@
+// Krylov solvers on device-resident vectors: Lanczos ground state (with an
+// optional fully reorthogonalized variant) and Freund's band Lanczos.
+// The host keeps only the scalars (alpha, beta, the projected matrix) and the
+// control flow; every length-dim vector stays in HBM.
+#include <cusolverDn.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <random>
+
+#include "qcmg_blas.h"
+#include "qcmg_internal.h"
+#include "qcmg_krylov.h"
+#include "qcmg_tridiag.h"
+
+namespace qcmg {
+
+// ---------------------------------------------------------------------------
+// multi-vector kernels used by reorthogonalization and band Lanczos
+
+constexpr int kTile = 2048;  // elements of w staged per block iteration
+
+// part[b*m + k] = sum over block b's tiles of V_k . w
+__global__ void __launch_bounds__(256) k_multidot(const double* const* __restrict__ V, int m,
+                                                  const double* __restrict__ w, size_t n,
+                                                  double* __restrict__ part) {
+  __shared__ double ws[kTile];
+  extern __shared__ double acc[];  // m accumulators
+  for (int k = threadIdx.x; k < m; k += blockDim.x) acc[k] = 0.0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  for (size_t base = (size_t)blockIdx.x * kTile; base < n; base += (size_t)gridDim.x * kTile) {
+    const size_t len = min((size_t)kTile, n - base);
+    __syncthreads();
+    for (size_t i = threadIdx.x; i < len; i += blockDim.x) ws[i] = w[base + i];
+    __syncthreads();
+    for (int k = warp; k < m; k += nwarp) {
+      const double* vk = V[k] + base;
+      double s = 0.0;
+      for (size_t i = lane; i < len; i += 32) s = fma(vk[i], ws[i], s);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lane == 0) acc[k] += s;  // warp k%nwarp owns acc[k]: no race
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += blockDim.x) part[(size_t)blockIdx.x * m + k] = acc[k];
+}
+
+// out[k] = sum_b part[b*m + k], fixed order.
+__global__ void k_multidot_final(const double* __restrict__ part, int nb, int m,
+                                 double* __restrict__ out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < m; k += gridDim.x * blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nb; ++b) s += part[(size_t)b * m + k];
+    out[k] = s;
+  }
+}
+
+// w -= sum_k c_k V_k
+__global__ void __launch_bounds__(256) k_multiaxpy(const double* const* __restrict__ V, int m,
+                                                   const double* __restrict__ c,
+                                                   double* __restrict__ w, size_t n) {
+  extern __shared__ double cs[];
+  for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = c[k];
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double s = w[i];
+    for (int k = 0; k < m; ++k) s = fma(-cs[k], V[k][i], s);
+    w[i] = s;
+  }
+}
+
+struct MultiOps {
+  DevBuf<const double*> ptrs;
+  DevBuf<double> part, coef;
+  std::vector<double> host;
+  int nblocks = 0;
+  void multidot(const std::vector<const double*>& V, const double* w, size_t n, cudaStream_t s,
+                std::vector<double>& out) {
+    const int m = (int)V.size();
+    out.assign(m, 0.0);
+    if (m == 0) return;
+    nblocks = (int)std::min<size_t>((n + kTile - 1) / kTile, 2 * 152);
+    if (nblocks < 1) nblocks = 1;
+    ptrs.alloc(m);
+    QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+    part.alloc((size_t)nblocks * m);
+    coef.alloc(m);
+    k_multidot<<<nblocks, 256, m * sizeof(double), s>>>(ptrs.p, m, w, n, part.p);
+    k_multidot_final<<<(m + 127) / 128, 128, 0, s>>>(part.p, nblocks, m, coef.p);
+    QCMG_CUDA(cudaGetLastError());
+    QCMG_CUDA(cudaMemcpyAsync(out.data(), coef.p, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+  }
+  void multiaxpy(const std::vector<const double*>& V, const std::vector<double>& c, double* w,
+                 size_t n, cudaStream_t s) {
+    const int m = (int)V.size();
+    if (m == 0 || n == 0) return;
+    ptrs.alloc(m);
+    coef.alloc(m);
+    QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+    QCMG_CUDA(cudaMemcpyAsync(coef.p, c.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+    size_t g = std::min<size_t>((n + 255) / 256, 152 * 8);
+    k_multiaxpy<<<(unsigned)std::max<size_t>(g, 1), 256, m * sizeof(double), s>>>(ptrs.p, m,
+                                                                                   coef.p, w, n);
+    QCMG_CUDA(cudaGetLastError());
+  }
+};
+
+// ---------------------------------------------------------------------------
+
+void seeded_vector(size_t dim, unsigned seed, double* out) {
+  std::normal_distribution<double> dist(0.0, 1.0);
+  std::default_random_engine gen(seed);
+  double s = 0.0;
+  for (size_t i = 0; i < dim; ++i) {
+    out[i] = dist(gen);
+    s += out[i] * out[i];
+  }
+  s = 1.0 / std::sqrt(s);
+  for (size_t i = 0; i < dim; ++i) out[i] *= s;
+}
+
+static void dalloc(double** p, size_t n) { QCMG_CUDA(cudaMalloc(p, std::max<size_t>(n, 1) * 8)); }
+
+struct DevVec {
+  double* p = nullptr;
+  DevVec() = default;
+  explicit DevVec(size_t n) { dalloc(&p, n); }
+  DevVec(const DevVec&) = delete;
+  DevVec(DevVec&& o) noexcept : p(o.p) { o.p = nullptr; }
+  ~DevVec() {
+    if (p) cudaFree(p);
+  }
+};
+
+LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,
+                                   double tol, int max_iter, int reorth, double* psi_host) {
+  const size_t n = H->dim;
+  cudaStream_t s = H->stream;
+  LanczosResult res;
+  QCMG_CHECK_ARG(n > 0, "empty sector");
+  std::vector<double> hx0;
+  if (!x0_host) {
+    hx0.resize(n);
+    seeded_vector(n, seed, hx0.data());
+    x0_host = hx0.data();
+  }
+  DevVec x0(n), r(n), q(n);
+  QCMG_CUDA(cudaMemcpyAsync(x0.p, x0_host, n * 8, cudaMemcpyHostToDevice, s));
+  QCMG_CUDA(cudaMemcpyAsync(r.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+  QCMG_CUDA(cudaMemsetAsync(q.p, 0, n * 8, s));
+  Reducer red;
+  std::vector<double> z;
+  double* rp = r.p;
+  double* qp = q.p;
+
+  if (reorth <= 0) {
+    // Three-term recurrence of LanczosEigenvalue (Lanczos.hpp:64-93).
+    double ritz = 2.0 * tol;
+    while (ritz > tol) {
+      if (!res.beta.empty()) scale2(rp, 1.0 / res.beta.back(), qp, -res.beta.back(), n, s);
+      matvec(H, rp, qp, true);
+      std::swap(rp, qp);
+      double a = red.dot(qp, rp, n, s);
+      res.alpha.push_back(a);
+      double b2 = red.axpy_norm2(rp, qp, a, n, s);
+      res.beta.push_back(std::sqrt(b2));
+      res.energy = tridiag_lowest(res.alpha, res.beta, z);
+      ritz = std::fabs(z.back() * res.beta.back());
+      if (!std::isfinite(res.energy) || !std::isfinite(ritz))
+        throw Error(QCMG_ERR_NUMERIC, "Lanczos produced a non-finite value");
+      if ((int)res.alpha.size() > max_iter)
+        throw Error(QCMG_ERR_NOCONV,
+                    "Lanczos procedure exceeded " + std::to_string(max_iter) + " iterations");
+    }
+    res.niter = (int)res.alpha.size();
+    if (psi_host) {
+      // Eigenvector replay of LanczosEigenvector (Lanczos.hpp:109-131).
+      DevVec gs(n);
+      QCMG_CUDA(cudaMemcpyAsync(gs.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+      scale(gs.p, z[0], n, s);
+      QCMG_CUDA(cudaMemcpyAsync(r.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+      QCMG_CUDA(cudaMemsetAsync(q.p, 0, n * 8, s));
+      for (size_t j = 1; j < z.size(); ++j) {
+        matvec(H, r.p, q.p, true);
+        replay_step(r.p, q.p, gs.p, res.alpha[j - 1], res.beta[j - 1], z[j], n, s);
+      }
+      QCMG_CUDA(cudaMemcpyAsync(psi_host, gs.p, n * 8, cudaMemcpyDeviceToHost, s));
+      QCMG_CUDA(cudaStreamSynchronize(s));
+    }
+    return res;
+  }
+
+  // Fully reorthogonalized Lanczos: the basis is kept in HBM and every new
+  // residual is projected out of it twice (classical Gram-Schmidt x2).
+  std::vector<DevVec> V;
+  std::vector<const double*> Vp;
+  MultiOps mops;
+  std::vector<double> c;
+  V.emplace_back(n);
+  QCMG_CUDA(cudaMemcpyAsync(V[0].p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+  Vp.push_back(V[0].p);
+  double* w = r.p;  // residual
+  double ritz = 2.0 * tol;
+  for (int j = 0; ritz > tol; ++j) {
+    QCMG_CUDA(cudaMemsetAsync(w, 0, n * 8, s));
+    matvec(H, V[j].p, w, true);
+    if (j > 0) axpy(w, V[j - 1].p, -res.beta.back(), n, s);
+    double a = red.dot(V[j].p, w, n, s);
+    res.alpha.push_back(a);
+    axpy(w, V[j].p, -a, n, s);
+    for (int pass = 0; pass < 2; ++pass) {
+      mops.multidot(Vp, w, n, s, c);
+      mops.multiaxpy(Vp, c, w, n, s);
+    }
+    double b = std::sqrt(red.dot(w, w, n, s));
+    res.beta.push_back(b);
+    res.energy = tridiag_lowest(res.alpha, res.beta, z);
+    ritz = std::fabs(z.back() * b);
+    if (!std::isfinite(res.energy) || !std::isfinite(ritz))
+      throw Error(QCMG_ERR_NUMERIC, "Lanczos produced a non-finite value");
+    if (ritz <= tol || b == 0.0) break;
+    if ((int)V.size() >= reorth || j + 1 >= max_iter)
+      throw Error(QCMG_ERR_NOCONV, "reorthogonalized Lanczos did not converge within " +
+                                       std::to_string(V.size()) + " stored vectors");
+    V.emplace_back(n);
+    QCMG_CUDA(cudaMemcpyAsync(V.back().p, w, n * 8, cudaMemcpyDeviceToDevice, s));
+    scale(V.back().p, 1.0 / b, n, s);
+    Vp.push_back(V.back().p);
+  }
+  res.niter = (int)res.alpha.size();
+  if (psi_host) {
+    DevVec gs(n);
+    QCMG_CUDA(cudaMemsetAsync(gs.p, 0, n * 8, s));
+    std::vector<const double*> Vz(Vp.begin(), Vp.begin() + z.size());
+    std::vector<double> mz(z.size());
+    for (size_t k = 0; k < z.size(); ++k) mz[k] = -z[k];
+    mops.multiaxpy(Vz, mz, gs.p, n, s);
+    QCMG_CUDA(cudaMemcpyAsync(psi_host, gs.p, n * 8, cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+  }
+  return res;
+}
+
+// ---------------------------------------------------------------------------
+// Band Lanczos (Freund), as in src_ed/Hamiltonian/Lanczos.hpp:214-395.
+
+struct Cusolver {
+  cusolverDnHandle_t h = nullptr;
+  DevBuf<double> A, W, work;
+  DevBuf<int> info;
+  ~Cusolver() {
+    if (h) cusolverDnDestroy(h);
+  }
+  // Eigen-decomposition of the leading j x j block of column-major t (ld).
+  void syevd(const std::vector<double>& t, int ld, int j, bool vectors, cudaStream_t s,
+             std::vector<double>& evals, std::vector<double>* U) {
+    if (!h) {
+      if (cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS)
+        throw Error(QCMG_ERR_CUDA, "cusolverDnCreate failed");
+    }
+    cusolverDnSetStream(h, s);
+    std::vector<double> a((size_t)j * j);
+    for (int c = 0; c < j; ++c)
+      for (int r = 0; r < j; ++r) a[r + (size_t)j * c] = t[r + (size_t)ld * c];
+    A.upload(a.data(), a.size(), s);
+    W.alloc(j);
+    info.alloc(1);
+    auto jobz = vectors ? CUSOLVER_EIG_MODE_VECTOR : CUSOLVER_EIG_MODE_NOVECTOR;
+    int lwork = 0;
+    if (cusolverDnDsyevd_bufferSize(h, jobz, CUBLAS_FILL_MODE_LOWER, j, A.p, j, W.p, &lwork) !=
+        CUSOLVER_STATUS_SUCCESS)
+      throw Error(QCMG_ERR_CUDA, "cusolverDnDsyevd_bufferSize failed");
+    work.alloc(std::max(lwork, 1));
+    if (cusolverDnDsyevd(h, jobz, CUBLAS_FILL_MODE_LOWER, j, A.p, j, W.p, work.p, lwork,
+                         info.p) != CUSOLVER_STATUS_SUCCESS)
+      throw Error(QCMG_ERR_CUDA, "cusolverDnDsyevd failed");
+    int hinfo = 0;
+    evals.resize(j);
+    QCMG_CUDA(cudaMemcpyAsync(&hinfo, info.p, sizeof(int), cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaMemcpyAsync(evals.data(), W.p, j * 8, cudaMemcpyDeviceToHost, s));
+    if (U) {
+      U->resize((size_t)j * j);
+      QCMG_CUDA(cudaMemcpyAsync(U->data(), A.p, (size_t)j * j * 8, cudaMemcpyDeviceToHost, s));
+    }
+    QCMG_CUDA(cudaStreamSynchronize(s));
+    if (hinfo != 0) throw Error(QCMG_ERR_NUMERIC, "syevd did not converge");
+  }
+};
+
+BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int M0, int max_iter,
+                        double acc_defl, double acc_band) {
+  const size_t n = H->dim;
+  cudaStream_t s = H->stream;
+  BandResult out;
+  QCMG_CHECK_ARG(p > 0, "band Lanczos needs at least one start vector");
+  int pc = p;
+  if (M0 > max_iter) M0 = max_iter;
+  int M0p = (M0 / p + 1) * p;
+  M0 = M0p - pc;
+  QCMG_CHECK_ARG(M0 > 0, "band Lanczos needs M > 0");
+  // Device vectors: the p start vectors plus a pool for v[0..M0p).
+  std::vector<DevVec> phi;
+  std::vector<const double*> phip;
+  for (int k = 0; k < p; ++k) {
+    phi.emplace_back(n);
+    QCMG_CUDA(cudaMemcpyAsync(phi[k].p, phi_host + (size_t)k * n, n * 8, cudaMemcpyHostToDevice,
+                              s));
+    phip.push_back(phi[k].p);
+  }
+  std::vector<double*> v(M0p, nullptr);
+  std::vector<double*> pool;
+  std::vector<DevVec> owned;
+  auto get = [&]() -> double* {
+    if (!pool.empty()) {
+      double* r = pool.back();
+      pool.pop_back();
+      return r;
+    }
+    owned.emplace_back(n);
+    return owned.back().p;
+  };
+  auto erase = [&](int k) {
+    if (v[k]) pool.push_back(v[k]);
+    v[k] = nullptr;
+  };
+  for (int i = 0; i < p; ++i) {
+    v[i] = get();
+    QCMG_CUDA(cudaMemcpyAsync(v[i], phi[i].p, n * 8, cudaMemcpyDeviceToDevice, s));
+  }
+  std::vector<double> t((size_t)M0 * M0, 0.0);  // column-major t(r,c) = t[r + M0*c]
+  auto T = [&](int r, int c) -> double& { return t[(size_t)r + (size_t)M0 * c]; };
+  std::vector<double> P((size_t)p * M0, 0.0);   // P(k,j) = P[k + p*j]
+  std::vector<int> defl(M0, 0);
+  std::vector<int> I;
+  Reducer red;
+  MultiOps mops;
+  std::vector<double> tmp;
+  Cusolver solver;
+  double ev_old = 1e12;
+  int j;
+  for (j = 0; j < M0; ++j) {
+    double z = std::sqrt(red.dot(v[j], v[j], n, s));
+    if (z < acc_defl) {
+      if (j >= pc) {
+        I.push_back(j - pc);
+        defl[j - pc] = 1;
+      }
+      pc--;
+      if (pc == 0) break;
+      erase(j);
+      for (int k = j; k < j + pc; ++k) v[k] = v[k + 1];
+      v[j + pc] = nullptr;
+      j--;
+      continue;
+    }
+    scale(v[j], 1.0 / z, n, s);
+    if (j >= pc) T(j, j - pc) = z;
+    mops.multidot(phip, v[j], n, s, tmp);
+    for (int k = 0; k < p; ++k) P[k + (size_t)p * j] = tmp[k];
+    for (int k = j + 1; k < j + pc; ++k) {
+      double zz = red.dot(v[j], v[k], n, s);
+      axpy(v[k], v[j], -zz, n, s);
+      if (k >= pc) T(j, k - pc) = zz;
+    }
+    v[j + pc] = get();
+    QCMG_CUDA(cudaMemsetAsync(v[j + pc], 0, n * 8, s));
+    matvec(H, v[j], v[j + pc], true);
+    int k0 = 0;
+    if (j > pc) {
+      k0 = j - pc;
+      if (defl[k0 - 1] == 0) erase(k0 - 1);
+    }
+    for (int k = k0; k < j; ++k) {
+      T(k, j) = T(j, k);
+      axpy(v[j + pc], v[k], -T(k, j), n, s);
+    }
+    for (int idx : I) {
+      double w = red.dot(v[idx], v[j + pc], n, s);
+      axpy(v[j + pc], v[idx], -w, n, s);
+      T(idx, j) = w;
+    }
+    double w = red.dot(v[j], v[j + pc], n, s);
+    axpy(v[j + pc], v[j], -w, n, s);
+    T(j, j) = w;
+    for (int idx : I) T(j, idx) = T(idx, j);
+    if (j >= 4 * p && j % p == 0) {
+      std::vector<double> ev;
+      solver.syevd(t, M0, j, false, s, ev, nullptr);
+      double test = std::fabs(ev[0] - ev_old);
+      ev_old = ev[0];
+      if (test < acc_band) break;
+    }
+  }
+  out.M = j;
+  if (j == 0) return out;
+  std::vector<double> U;
+  solver.syevd(t, M0, j, true, s, out.evals, &U);
+  // Q = P(:, 0:k) U(0:k, :), k = min(p, M) (Hamiltonian_base.hpp:249 with
+  // matrix::product's bound on the inner index).
+  const int M = j, kk = std::min(p, M);
+  out.Q.assign((size_t)p * M, 0.0);
+  for (int a = 0; a < p; ++a)
+    for (int c = 0; c < M; ++c) {
+      double acc = 0.0;
+      for (int k = 0; k < kk; ++k) acc += P[a + (size_t)p * k] * U[k + (size_t)M * c];
+      out.Q[(size_t)a * M + c] = acc;
+    }
+  return out;
+}
+
+}  // namespace qcmg

@@ -1,0 +1,36 @@
+// Krylov solver drivers (host control flow, device vectors).
+#pragma once
+
+#include <vector>
+
+#include "qcmg_internal.h"
+
+namespace qcmg {
+
+struct LanczosResult {
+  std::vector<double> alpha, beta;
+  double energy = 0.0;
+  int niter = 0;
+};
+
+struct BandResult {
+  int M = 0;
+  std::vector<double> evals;  // M
+  std::vector<double> Q;      // p x M, row-major
+};
+
+void seeded_vector(size_t dim, unsigned seed, double* out);
+
+LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,
+                                   double tol, int max_iter, int reorth, double* psi_host);
+
+BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int M0, int max_iter,
+                        double acc_defl, double acc_band);
+
+void launch_apply_c(int L, int orb, int spin, int pm, int nup, int ndn, const double* x, double* y,
+                    double z, bool accumulate, cudaStream_t s);
+
+void green_function_batch(int L, int M, const double* e, const double* v, int nz, const double* z,
+                          double* G, cudaStream_t s);
+
+}  // namespace qcmg

@@ -1,0 +1,479 @@
+"""Cluster exact-diagonalization layer on the GPU engine.
+
+Mirrors the part of pyqcm's ED interface that sits on the factorized hot
+path, with the same names and argument meanings:
+  ClusterModel      ~ ED::new_model / ED::new_operator (src_ed/qcm_ED.hpp:34-78)
+  Hamiltonian       ~ Hamiltonian<HF> in a new format 'G'
+                      (src_ed/Hamiltonian/Hamiltonian_base.hpp:43-82):
+                      mult_add, states, GS_energy, build_Q_matrix
+  ModelInstance     ~ model_instance<HF> (src_ed/model_instance.hpp):
+                      ground_state (low_energy_states), Green_function_solve
+                      (build_qmatrix), Green_function, qmatrix,
+                      hybridization_function, self_energy, Potthoff_functional
+Every vector operation runs in libqcmg (no CPU fallback); the host keeps the
+small dense pieces (Q-matrix assembly, hopping matrices).
+"""
+import math
+
+import numpy as np
+
+from . import _lib
+from ._lib import QcmgError, as_f64, check, lib, ptr
+
+# Global parameters with the reference's defaults (src_util/global_parameter.cpp:17-90).
+GLOBAL = {
+    "accur_lanczos": 1e-12,
+    "max_iter_lanczos": 1000,
+    "accur_band_lanczos": 1e-12,
+    "accur_deflation": 1e-7,
+    "max_iter_BL": 600,
+    "accur_Q_matrix": 1e-5,
+    "Qmatrix_wtol": 1e-5,
+    "Qmatrix_vtol": 1e-10,
+    "minimum_weight": 0.01,
+    "temperature": 0.0,
+    "seed": 0,
+    "Lanczos_reorth": 0,
+}
+MIN_GAP = 1.0e-6      # src_ed/model.hpp:19
+SMALL_VALUE = 1e-12   # degeneracy threshold of compute_weights
+
+
+def set_global_parameter(name, value):
+    if name not in GLOBAL:
+        raise ValueError(f"unknown global parameter {name}")
+    GLOBAL[name] = type(GLOBAL[name])(value)
+
+
+class Sector:
+    """Sector "R0:N8:S0": N electrons, S = 2 Sz (src_ed/sector.hpp:36-95)."""
+
+    def __init__(self, s):
+        parts = dict((p[0], int(p[1:])) for p in s.split(":"))
+        if parts.get("R", 0) != 0:
+            raise ValueError("the factorized format has a trivial point group: only R0 sectors")
+        self.N, self.S = parts["N"], parts["S"]
+        if (self.N + self.S) % 2:
+            raise ValueError(f"invalid sector {s}")
+        self.nup, self.ndn = (self.N + self.S) // 2, (self.N - self.S) // 2
+
+    @staticmethod
+    def of(nup, ndn):
+        return Sector(f"R0:N{nup + ndn}:S{nup - ndn}")
+
+    def name(self):
+        return f"R0:N{self.N}:S{self.S}"
+
+    def __repr__(self):
+        return self.name()
+
+
+class ClusterModel:
+    """Cluster (impurity) model: n_sites cluster orbitals + n_bath bath
+    orbitals; spin-orbital r < n_orb is up, r >= n_orb is down."""
+
+    def __init__(self, n_sites, n_bath=0, name="clus"):
+        self.name, self.n_sites, self.n_bath = name, n_sites, n_bath
+        self.n_orb = n_sites + n_bath
+        if self.n_orb > 32:
+            raise ValueError("at most 32 orbitals per spin")
+        self.operators = {}
+
+    def new_operator(self, name, op_type, elements):
+        if op_type not in ("one-body", "interaction"):
+            raise ValueError("only one-body and density-density interaction operators factorize")
+        self.operators[name] = (op_type, [(int(r), int(c), float(v)) for r, c, v in elements])
+
+    def combine(self, values):
+        """Hops per spin and density-density pairs of the value map.  One-body
+        elements keep r <= c and add the conjugate of r < c
+        (src_ed/Operators/one_body_operator.hpp:62-71)."""
+        hop, pairs = {}, {}
+        n = self.n_orb
+        for name, coef in values.items():
+            if name not in self.operators or coef == 0.0:
+                continue
+            typ, els = self.operators[name]
+            for r, c, v in els:
+                if typ == "interaction":
+                    key = (min(r, c), max(r, c))
+                    pairs[key] = pairs.get(key, 0.0) + coef * v
+                elif r <= c:
+                    hop[(r, c)] = hop.get((r, c), 0.0) + coef * v
+                    if r != c:
+                        hop[(c, r)] = hop.get((c, r), 0.0) + coef * v
+        up, dn = [], []
+        for (r, c), v in sorted(hop.items()):
+            if r < n and c < n:
+                up.append((r, c, v))
+            elif r >= n and c >= n:
+                dn.append((r - n, c - n, v))
+            else:
+                raise ValueError("spin-flip terms do not factorize")
+        return up, dn, [(r, c, v) for (r, c), v in sorted(pairs.items())]
+
+    def one_body_matrix(self, values, spin_down=False):
+        up, dn, _ = self.combine(values)
+        T = np.zeros((self.n_orb, self.n_orb))
+        for r, c, v in (dn if spin_down else up):
+            T[r, c] += v
+        return T
+
+
+def _arrays(els):
+    r = np.array([e[0] for e in els], np.int32)
+    c = np.array([e[1] for e in els], np.int32)
+    v = np.array([e[2] for e in els], np.float64)
+    return r, c, v
+
+
+class State:
+    def __init__(self, sector, energy, psi):
+        self.sec, self.energy, self.psi = sector, energy, psi
+        self.weight = 1.0
+        self.gf = None
+        self.gf_down = None
+
+
+class Hamiltonian:
+    """Factorized Hamiltonian of one sector on the GPU (format 'G')."""
+
+    def __init__(self, model, values, sector):
+        self.model = model
+        self.sec = sector if isinstance(sector, Sector) else Sector(sector)
+        up, dn, pairs = model.combine(values)
+        L = model.n_orb
+        ur, uc, uv = _arrays(up)
+        dr, dc, dv = _arrays(dn)
+        pr, pc, pv = _arrays(pairs)
+        h = _lib.vp()
+        check(lib().qcmg_hamiltonian_create(L, self.sec.nup, self.sec.ndn,
+                                            len(up), ptr(ur), ptr(uc), ptr(uv),
+                                            len(dn), ptr(dr), ptr(dc), ptr(dv),
+                                            len(pairs), ptr(pr), ptr(pc), ptr(pv), h))
+        self._h = h
+        du, dd, dim = _lib.c_size_t(), _lib.c_size_t(), _lib.c_size_t()
+        check(lib().qcmg_hamiltonian_dims(h, du, dd, dim))
+        self.dim_up, self.dim_dn, self.dim = du.value, dd.value, dim.value
+
+    def __del__(self):
+        h = getattr(self, "_h", None)
+        if h is not None and _lib._lib is not None:
+            _lib._lib.qcmg_hamiltonian_destroy(h)
+            self._h = None
+
+    def mult_add(self, x, y):
+        """y += H x (host numpy vectors, y modified in place)."""
+        x = as_f64(x)
+        assert y.dtype == np.float64 and y.flags.c_contiguous and y.shape == (self.dim,)
+        check(lib().qcmg_matvec(self._h, ptr(x), ptr(y), _lib.QCMG_ACCUMULATE))
+
+    def matvec(self, x):
+        y = np.zeros(self.dim)
+        check(lib().qcmg_matvec(self._h, ptr(as_f64(x)), ptr(y), 0))
+        return y
+
+    def matvec_device(self, x_ptr, y_ptr, accumulate=False, asynchronous=False):
+        """y (+)= H x on device pointers (e.g. torch CUDA tensors' data_ptr())."""
+        flags = _lib.QCMG_DEVICE_PTRS | (_lib.QCMG_ACCUMULATE if accumulate else 0)
+        if asynchronous:
+            flags |= _lib.QCMG_ASYNC
+        check(lib().qcmg_matvec(self._h, x_ptr, y_ptr, flags))
+
+    def set_stream(self, stream_ptr):
+        """Launch on a caller-owned cudaStream_t (int handle, 0 = own stream)."""
+        check(lib().qcmg_hamiltonian_set_stream(self._h, stream_ptr or None))
+
+    def halfop(self, spin):
+        nnz = _lib.c_size_t()
+        check(lib().qcmg_hamiltonian_halfop(self._h, spin, nnz, None, None, None, None))
+        dim = self.dim_dn if spin else self.dim_up
+        rp = np.zeros(dim + 1, np.uint32)
+        col = np.zeros(max(nnz.value, 1), np.uint32)
+        val = np.zeros(max(nnz.value, 1))
+        diag = np.zeros(max(dim, 1))
+        check(lib().qcmg_hamiltonian_halfop(self._h, spin, nnz, ptr(rp), ptr(col), ptr(val),
+                                            ptr(diag)))
+        return rp, col[: nnz.value], val[: nnz.value], diag[:dim]
+
+    def lanczos(self, x0=None, tol=None, max_iter=None, reorth=None, want_psi=True):
+        """Returns (E0, psi, alpha, beta)."""
+        tol = GLOBAL["accur_lanczos"] if tol is None else tol
+        max_iter = GLOBAL["max_iter_lanczos"] if max_iter is None else max_iter
+        reorth = GLOBAL["Lanczos_reorth"] if reorth is None else reorth
+        cap = max_iter + 2
+        alpha, beta = np.zeros(cap), np.zeros(cap)
+        psi = np.zeros(self.dim) if want_psi else None
+        e0, nit = _lib.c_double(), _lib.c_int()
+        x0a = None if x0 is None else as_f64(x0)
+        check(lib().qcmg_lanczos_ground_state(self._h, ptr(x0a), GLOBAL["seed"], tol, max_iter,
+                                              reorth, e0, ptr(psi), nit, ptr(alpha), ptr(beta),
+                                              cap))
+        n = nit.value
+        return e0.value, psi, alpha[:n], beta[:n]
+
+    def GS_energy(self):
+        return self.lanczos(want_psi=False)[0]
+
+    def states(self, GS_energy=1.0e12):
+        """Lanczos ground state of this sector (Hamiltonian::states, method 'L').
+        Returns ([State], updated GS_energy)."""
+        if self.dim == 0:
+            return [], GS_energy
+        e0, psi, _, _ = self.lanczos()
+        GS_energy = min(GS_energy, e0)
+        out = []
+        if e0 - GS_energy <= max(MIN_GAP, 0.0):
+            out.append(State(self.sec, e0, psi))
+        return out, GS_energy
+
+    def build_Q_matrix(self, phi):
+        """(e, Q) with Q of shape (p, M) (Hamiltonian_base.hpp:229-254)."""
+        p = len(phi)
+        if self.dim == 0 or p == 0:
+            return np.zeros(0), np.zeros((p, 0))
+        M = int(14 * p * math.log(1.0 * self.dim))
+        if M <= 1:
+            M = 2
+        phis = np.ascontiguousarray(np.array(phi, np.float64).reshape(p, self.dim))
+        cap = GLOBAL["max_iter_BL"] + 2 * p + 2
+        ev = np.zeros(cap)
+        Q = np.zeros(p * cap)
+        Mo = _lib.c_int()
+        check(lib().qcmg_band_lanczos(self._h, p, ptr(phis), M, GLOBAL["max_iter_BL"],
+                                      GLOBAL["accur_deflation"], GLOBAL["accur_band_lanczos"],
+                                      Mo, ptr(ev), ptr(Q), cap))
+        m = Mo.value
+        return ev[:m].copy(), Q[: p * m].reshape(p, m).copy()
+
+
+def apply_c(L, orb, pm, nup, ndn, x, z=1.0):
+    """c_orb (pm=-1) / c^dagger_orb (pm=+1) applied to x on the GPU."""
+    spin = orb >= L
+    nup2, ndn2 = nup + (0 if spin else pm), ndn + (pm if spin else 0)
+    if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
+        return np.zeros(0)
+    n2 = math.comb(L, nup2) * math.comb(L, ndn2)
+    y = np.zeros(n2)
+    check(lib().qcmg_apply_c(L, orb, pm, nup, ndn, ptr(as_f64(x)), ptr(y), z, 0))
+    return y
+
+
+def halfbasis(L, N):
+    d = _lib.c_size_t()
+    check(lib().qcmg_halfbasis(L, N, None, 0, d))
+    out = np.zeros(max(d.value, 1), np.uint32)
+    check(lib().qcmg_halfbasis(L, N, ptr(out), d.value, d))
+    return out[: d.value]
+
+
+def halfbasis_rank(L, N, states):
+    st = np.ascontiguousarray(states, np.uint32)
+    out = np.zeros(max(len(st), 1), np.uint32)
+    check(lib().qcmg_halfbasis_rank(L, N, ptr(st), len(st), ptr(out)))
+    return out[: len(st)]
+
+
+def green_function(e, v, z):
+    """G for a list of complex frequencies; v is (L, M) complex.  Returns
+    (nz, L, L) in the reference's orientation G[w][b, a] (as numpy [b, a])."""
+    e = as_f64(e)
+    v = np.asarray(v, np.complex128)
+    L, M = v.shape
+    zs = np.atleast_1d(np.asarray(z, np.complex128))
+    vv = np.ascontiguousarray(v.T).view(np.float64).reshape(-1)   # column-major (a + L i)
+    zz = np.ascontiguousarray(zs).view(np.float64)
+    G = np.zeros(2 * L * L * len(zs))
+    check(lib().qcmg_green_function(L, M, ptr(e), ptr(vv), len(zs), ptr(zz), ptr(G)))
+    Gc = G.view(np.complex128).reshape(len(zs), L, L)   # [w][a][b] = G[b + a L]
+    return np.transpose(Gc, (0, 2, 1)).copy()           # numpy [b, a]
+
+
+def streamline(e, v, wtol=None, vtol=None):
+    """Merges degenerate poles (src_ed/Q_matrix.hpp:180-223).  v is (L, M)."""
+    wtol = GLOBAL["Qmatrix_wtol"] if wtol is None else wtol
+    vtol = GLOBAL["Qmatrix_vtol"] if vtol is None else vtol
+    L, M = v.shape
+    if vtol < 1e-12:
+        return e, v
+    e2, cols = [], []
+    i = 0
+    while i < M:
+        j = i + 1
+        while j < M and abs(e[j] - e[i]) <= wtol:
+            j += 1
+        if j - i == 1:
+            if np.sum(np.abs(v[:, i]) ** 2) >= vtol:
+                e2.append(e[i])
+                cols.append(v[:, i])
+        else:
+            Q = v[:, i:j]
+            d, U = np.linalg.eigh(Q @ Q.conj().T)
+            for k in range(L):
+                if d[k] > vtol:
+                    e2.append(e[i])
+                    cols.append(U[:, k] * math.sqrt(d[k]))
+        i = j
+    if not cols:
+        return np.zeros(0), np.zeros((L, 0), v.dtype)
+    return np.array(e2), np.array(cols).T
+
+
+class ModelInstance:
+    """Instance of a cluster model with parameter values and target sectors."""
+
+    def __init__(self, model, values, sectors, label=0):
+        self.model, self.label = model, label
+        self.values = {k: float(v) for k, v in values.items() if k in model.operators}
+        self.target_sectors = [Sector(s) for s in sectors.split("/")]
+        up, dn, _ = model.combine(self.values)
+        self.mixing = 4 if (sorted(up) != sorted(dn) or any(s.S for s in self.target_sectors)) else 0
+        self.gs_solved = self.gf_solved = False
+        self.states = []
+        self.GS_energy = None
+        self.E0 = None
+        self._H = {}
+
+    def hamiltonian(self, nup, ndn):
+        key = (nup, ndn)
+        if key not in self._H:
+            self._H[key] = Hamiltonian(self.model, self.values, Sector.of(nup, ndn))
+        return self._H[key]
+
+    def ground_state(self):
+        """(GS energy, sector string) -- model_instance::low_energy_states."""
+        if self.gs_solved:
+            return self.GS_energy, self._gs_string()
+        E = 1.0e12
+        states = []
+        for s in self.target_sectors:
+            H = self.hamiltonian(s.nup, s.ndn)
+            if H.dim == 0:
+                continue
+            st, E = H.states(E)
+            states += st
+        E0 = min(x.energy for x in states)
+        T = GLOBAL["temperature"]
+        if T < 1e-9:
+            states = [x for x in states if x.energy - E0 <= SMALL_VALUE]
+            for x in states:
+                x.weight = 1.0 / len(states)
+        else:
+            w = np.array([math.exp(-(x.energy - E0) / T) for x in states])
+            for x, wi in zip(states, w / w.sum()):
+                x.weight = wi
+        states = [x for x in states if x.weight >= GLOBAL["minimum_weight"]]
+        tot = sum(x.weight for x in states)
+        for x in states:
+            x.weight /= tot
+        if self.mixing == 0 and any(x.sec.S for x in states):
+            self.mixing = 4
+        self.states = states
+        self.GS_energy = min(x.energy for x in states)
+        self.E0 = sum(x.weight * x.energy for x in states)
+        self.gs_solved = True
+        return self.GS_energy, self._gs_string()
+
+    def _gs_string(self):
+        return "/".join(x.sec.name() for x in self.states)
+
+    def _qmatrix_state(self, st, spin_down):
+        L = self.model.n_orb
+        ns = self.model.n_sites
+        spin = 1 if spin_down else 0
+        blocks = {}
+        for pm in (-1, 1):
+            nup2 = st.sec.nup + (0 if spin else pm)
+            ndn2 = st.sec.ndn + (pm if spin else 0)
+            if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
+                continue
+            H = self.hamiltonian(nup2, ndn2)
+            if H.dim == 0:
+                continue
+            phi = [apply_c(L, o + spin * L, pm, st.sec.nup, st.sec.ndn, st.psi) for o in range(ns)]
+            e, Q = H.build_Q_matrix(phi)
+            e = e - st.energy
+            if pm == -1:
+                e = -e
+            e, Q = streamline(e, Q.astype(np.complex128))
+            if pm == 1:
+                Q = Q.conj()
+            blocks[pm] = (e, Q)
+        es = [blocks[pm][0] for pm in (-1, 1) if pm in blocks]
+        vs = [blocks[pm][1] for pm in (-1, 1) if pm in blocks]
+        e = np.concatenate(es) if es else np.zeros(0)
+        v = np.concatenate(vs, axis=1) if vs else np.zeros((ns, 0), np.complex128)
+        self._check_norm(v)
+        return e, v * math.sqrt(st.weight)
+
+    @staticmethod
+    def _check_norm(v):
+        D = v @ v.conj().T - np.eye(v.shape[0])
+        err = float(np.sum(np.abs(D) ** 2))
+        if err > GLOBAL["accur_Q_matrix"]:
+            raise QcmgError(-6, f"Q-matrix does not satisfy unitary condition by {err}")
+
+    def Green_function_solve(self):
+        if self.gf_solved:
+            return
+        self.ground_state()
+        for st in self.states:
+            st.gf = self._qmatrix_state(st, False)
+            if self.mixing & 4:
+                st.gf_down = self._qmatrix_state(st, True)
+        self.gf_solved = True
+
+    def qmatrix(self, spin_down=False):
+        """(e, v) of the first state, v of shape (L, M)."""
+        self.Green_function_solve()
+        st = self.states[0]
+        return st.gf_down if (spin_down and self.mixing & 4) else st.gf
+
+    def Green_function(self, z, spin_down=False):
+        """G(z) (n_sites x n_sites); z scalar or array (then (nz, L, L))."""
+        self.Green_function_solve()
+        zs = np.atleast_1d(np.asarray(z, np.complex128))
+        G = None
+        for st in self.states:
+            e, v = st.gf_down if (spin_down and self.mixing & 4) else st.gf
+            g = green_function(e, v, zs)
+            G = g if G is None else G + g
+        return G[0] if np.ndim(z) == 0 else G
+
+    def hopping_blocks(self, spin_down=False):
+        """(tc, tcb, tb) with the bath diagonalized (model_instance.hpp:425-475)."""
+        ns = self.model.n_sites
+        T = self.model.one_body_matrix(self.values, spin_down and bool(self.mixing & 4))
+        tc, tcb, tb = T[:ns, :ns], T[:ns, ns:], T[ns:, ns:]
+        if tb.size and np.count_nonzero(tb - np.diag(np.diag(tb))):
+            d, S = np.linalg.eigh(tb)
+            tb, tcb = np.diag(d), tcb @ S
+        return tc, tcb, tb
+
+    def hybridization_function(self, z, spin_down=False):
+        _, tcb, tb = self.hopping_blocks(spin_down)
+        ns = self.model.n_sites
+        G = np.zeros((ns, ns), np.complex128)
+        for i in range(tb.shape[0]):
+            G += np.outer(tcb[:, i], tcb[:, i].conj()) / (z - tb[i, i])
+        return G
+
+    def self_energy(self, z, spin_down=False):
+        G = self.Green_function(z, spin_down)
+        tc, _, _ = self.hopping_blocks(spin_down)
+        S = np.linalg.inv(G) + tc
+        if self.model.n_bath:
+            S = S + self.hybridization_function(z, spin_down)
+        return z * np.eye(len(tc)) - S
+
+    def SEF_bath(self):
+        sef = 0.0
+        for sd in ((False, True) if self.mixing & 4 else (False,)):
+            _, _, tb = self.hopping_blocks(sd)
+            sef -= sum(x for x in np.diag(tb) if x < 0)
+        return sef if self.mixing & 4 else 2.0 * sef
+
+    def Potthoff_functional(self):
+        """Cluster part E0 + SEF_bath (src_ed/qcm_ED.cpp:330-334)."""
+        self.Green_function_solve()
+        return self.E0 + self.SEF_bath()

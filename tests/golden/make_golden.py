@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
-from models import hubbard_cluster  # noqa: E402
+from models import CASES, ZS, hubbard_cluster  # noqa: E402
 
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "qcm_ref_driver")
 DT = {"f8": "<f8", "u4": "<u4", "c16": "<c16"}
@@ -78,29 +78,12 @@ def main():
     lines = ["halfbasis 8 4", "halfbasis 8 3", "halfbasis 12 6", "halfbasis 12 5", "halfbasis 16 8"]
     out = run_spec(lines)
     np.savez_compressed(os.path.join(HERE, "halfbasis.npz"), **out)
-    zs = [0.5j, 0.3 + 0.1j, -1.2 + 0.05j]
-    # 8-site open chain, t=1, U=4, mu=2, half filling (dim 4900).
-    sec = "R0:N8:S0"
-    ed_case("chain8", 8, 1, {"t": 1.0, "U": 4.0, "mu": 2.0}, sec,
-            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz",
-                   f"destroy clus {sec} 3 0 -1 dup", f"destroy clus {sec} 5 1 -1 ddn",
-                   f"destroy clus {sec} 2 0 1 cup", f"destroy clus {sec} 6 1 1 cdn"], gz=zs)
-    # Same chain in an odd sector with Sz = 1 (dims 56 x 35).
-    sec = "R0:N7:S1"
-    ed_case("chain8_n7", 8, 1, {"t": 1.0, "U": 4.0, "mu": 2.0}, sec,
-            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gf=False)
-    # 2x4 cluster with t' and a Neel field M: up and down half-operators differ.
-    sec = "R0:N8:S0"
-    ed_case("ladder2x4_af", 4, 2, {"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0, "M": 0.15}, sec,
-            af=True, extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gz=zs)
-    # 2x2 plaquette + 4 bath orbitals (8 orbitals, dim 4900).
-    params = {"t": 1.0, "U": 4.0, "mu": 2.0}
-    for k in range(4):
-        params[f"eb{k+1}"] = [-1.1, 0.7, 1.3, -0.4][k]
-        params[f"tb{k+1}"] = [0.5, 0.45, 0.6, 0.35][k]
-    ed_case("plaquette_bath4", 2, 2, params, sec, n_bath=4,
-            extra=[f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"], gz=zs)
-
+    for tag, (nx, ny, nb, af, params, sec, gf) in CASES.items():
+        extra = [f"hamiltonian clus {sec} h", f"lanczos clus {sec} lz"]
+        if tag == "chain8":
+            extra += [f"destroy clus {sec} 3 0 -1 dup", f"destroy clus {sec} 5 1 -1 ddn",
+                      f"destroy clus {sec} 2 0 1 cup", f"destroy clus {sec} 6 1 1 cdn"]
+        ed_case(tag, nx, ny, params, sec, n_bath=nb, af=af, extra=extra, gf=gf, gz=ZS)
 
 if __name__ == "__main__":
     main()

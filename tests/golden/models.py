@@ -58,3 +58,18 @@ def hubbard_cluster(nx, ny, n_bath=0, af=False):
         s = k % ns
         ops[f"tb{k+1}"] = ("one-body", [(s, b, 1.0), (s + no, b + no, 1.0)])
     return ns, n_bath, ops
+
+
+ZS = [0.5j, 0.3 + 0.1j, -1.2 + 0.05j]
+
+# Golden cases: (nx, ny, n_bath, af, params, sector, with_gf)
+CASES = {
+    "chain8": (8, 1, 0, False, {"t": 1.0, "U": 4.0, "mu": 2.0}, "R0:N8:S0", True),
+    "chain8_n7": (8, 1, 0, False, {"t": 1.0, "U": 4.0, "mu": 2.0}, "R0:N7:S1", False),
+    "ladder2x4_af": (4, 2, 0, True, {"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0, "M": 0.15},
+                     "R0:N8:S0", True),
+    "plaquette_bath4": (2, 2, 4, False,
+                        {"t": 1.0, "U": 4.0, "mu": 2.0, "eb1": -1.1, "eb2": 0.7, "eb3": 1.3,
+                         "eb4": -0.4, "tb1": 0.5, "tb2": 0.45, "tb3": 0.6, "tb4": 0.35},
+                        "R0:N8:S0", True),
+}

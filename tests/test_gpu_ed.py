@@ -1,0 +1,173 @@
+"""GPU parity of the exact-diagonalization path: the engine (libqcmg through
+its C ABI) against the reference's own outputs (tests/golden) and the CPU
+oracle on the same seeded inputs."""
+import math
+
+import numpy as np
+import pytest
+
+import qcm_oracle as qo
+from conftest import load_golden
+from helpers import case_model, csr_dense, engine_model, halfop_dense_from_ref, oracle_sector
+from models import CASES, ZS
+from test_oracle_golden import assert_qmatrix_parity
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def pg():
+    import pyqcm_gb300
+    pyqcm_gb300.lib()
+    return pyqcm_gb300
+
+
+def test_halfbasis_bit_exact(pg):
+    g = load_golden("halfbasis")
+    for key, ref in g.items():
+        if key.startswith("halfbasis_"):
+            _, L, N = key.split("_")
+            got = pg.halfbasis(int(L[1:]), int(N[1:]))
+            assert np.array_equal(got, ref), key
+    # larger and edge cases against the oracle
+    for L, N in ((16, 8), (20, 10), (24, 3), (5, 0), (5, 5), (1, 1)):
+        assert np.array_equal(pg.halfbasis(L, N), qo.halfbasis(L, N)), (L, N)
+
+
+def test_halfbasis_rank(pg):
+    bs = qo.halfbasis(16, 8)
+    assert np.array_equal(pg.halfbasis_rank(16, 8, bs), np.arange(len(bs), dtype=np.uint32))
+    # states outside the basis rank to dim
+    bad = np.array([0, 0xffff, 1 << 17, 0b111], np.uint32)
+    assert np.all(pg.halfbasis_rank(16, 8, bad) == len(bs))
+
+
+@pytest.mark.parametrize("tag", list(CASES))
+def test_halfop_tables_match_reference(pg, tag):
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    H = pg.Hamiltonian(m, params, sec)
+    ns, nb, ops, _, _ = case_model(tag)
+    names = [k for k in ops if ops[k][0] == "one-body" and k in params]
+    for spin, dim in ((0, H.dim_up), (1, H.dim_dn)):
+        sfx = "dn" if spin else "up"
+        T_ref = halfop_dense_from_ref(g, "h", [f"{n}_{sfx}" for n in names], params, dim)
+        T_gpu = csr_dense(*H.halfop(spin))
+        # index pattern bit-exact, values exact sums of the same doubles
+        assert np.array_equal(T_gpu != 0, T_ref != 0), (tag, spin)
+        assert np.allclose(T_gpu, T_ref, atol=1e-14, rtol=0), (tag, spin)
+
+
+@pytest.mark.parametrize("tag", list(CASES))
+def test_matvec_matches_reference(pg, tag):
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    H = pg.Hamiltonian(m, params, sec)
+    x = g["h_x0"]
+    y = H.matvec(x)
+    ref = g["h_Hx0"]
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+    # accumulate form: y += H x
+    y2 = np.ones(H.dim)
+    H.mult_add(x, y2)
+    assert np.max(np.abs(y2 - 1.0 - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+@pytest.mark.parametrize("tag", list(CASES))
+def test_lanczos_ground_state(pg, tag):
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    H = pg.Hamiltonian(m, params, sec)
+    e0, psi, al, be = H.lanczos()  # seeded start, as the reference's states()
+    assert abs(e0 - g["lz_E0"]) <= 1e-10 * abs(g["lz_E0"])
+    assert abs(len(al) - len(g["lz_alpha"])) <= 2
+    ov = abs(psi @ g["lz_psi"]) / (np.linalg.norm(psi) * np.linalg.norm(g["lz_psi"]))
+    assert ov > 1 - 1e-10
+    # first recurrence coefficients agree closely (before rounding drift)
+    assert np.max(np.abs(al[:10] - g["lz_alpha"][:10])) < 1e-10
+
+
+@pytest.mark.parametrize("tag", ["chain8", "ladder2x4_af"])
+def test_lanczos_reorth(pg, tag):
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    H = pg.Hamiltonian(m, params, sec)
+    e0, psi, al, be = H.lanczos(reorth=200)
+    assert abs(e0 - g["lz_E0"]) <= 1e-10 * abs(g["lz_E0"])
+    r = H.matvec(psi) - e0 * psi
+    assert np.linalg.norm(r) < 1e-8
+
+
+def test_create_destroy_bit_exact(pg):
+    g = load_golden("chain8")
+    for tag, orb, pm in (("dup", 3, -1), ("ddn", 5 + 8, -1), ("cup", 2, 1), ("cdn", 6 + 8, 1)):
+        y = pg.apply_c(8, orb, pm, 4, 4, g[tag + "_x"])
+        assert np.array_equal(y, g[tag + "_y"]), tag
+
+
+@pytest.mark.parametrize("tag", [t for t in CASES if CASES[t][6]])
+def test_green_function_pipeline(pg, tag):
+    """ground state -> c/c^dagger -> band Lanczos -> Q-matrix -> G(z), all on
+    the GPU, against the reference's Q-matrix and G(z)."""
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    inst = pg.ModelInstance(m, params, sec)
+    E0, gs_sec = inst.ground_state()
+    assert abs(E0 - g["gs_E0"]) <= 1e-10 * abs(g["gs_E0"])
+    af = CASES[tag][3]
+    for spin_down in ((False, True) if af else (False,)):
+        e, v = inst.qmatrix(spin_down)
+        q = "qdn" if spin_down else "qup"
+        assert_qmatrix_parity(e, v, g[q + "_e"], g[q + "_v"].T)
+        for k, z in enumerate(ZS):
+            G = inst.Green_function(z, spin_down)
+            ref = g[("gzdn" if spin_down else "gz") + str(k)]
+            assert np.max(np.abs(G - ref)) < 1e-8, (tag, spin_down, k)
+    assert abs(inst.Potthoff_functional() - g["omega"]) < 1e-8
+    if CASES[tag][2]:
+        for k, z in enumerate(ZS):
+            assert np.max(np.abs(inst.hybridization_function(z) - g[f"hyb{k}"])) < 1e-12
+            assert np.max(np.abs(inst.self_energy(z) - g[f"sig{k}"])) < 1e-7
+
+
+def test_green_function_kernel_vs_numpy(pg):
+    rng = np.random.default_rng(5)
+    L, M = 12, 700
+    e = np.sort(rng.uniform(-6, 6, M))
+    v = rng.normal(size=(L, M)) + 1j * rng.normal(size=(L, M))
+    zs = rng.uniform(-5, 5, 33) + 1j * rng.uniform(0.01, 2, 33)
+    G = pg.green_function(e, v, zs)
+    for w, z in enumerate(zs):
+        ref = qo.green_function(e, v, z)
+        assert np.max(np.abs(G[w] - ref)) < 1e-12 * np.max(np.abs(ref)) * 10
+
+
+def test_large_sector_matvec_vs_oracle(pg):
+    """3x4 cluster with t' at half filling (dim 853,776): engine vs oracle on
+    the same seeded vector."""
+    import models
+    ns, nb, ops = models.hubbard_cluster(4, 3)
+    params = {"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0}
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, params, "R0:N12:S0")
+    assert H.dim == 853776
+    up, dn, pr = qo.combine_terms(ops, params, ns)
+    S = qo.Sector(ns, 6, 6, up, dn, pr)
+    x = qo.seeded_start(H.dim, 3)
+    y = H.matvec(x)
+    ref = S.matvec(x, nthreads=8)
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_errors(pg):
+    m, params, sec = engine_model("chain8")
+    with pytest.raises(ValueError):
+        pg.Sector("R0:N7:S0")
+    with pytest.raises(pg.QcmgError):
+        pg.apply_c(8, 99, 1, 4, 4, np.zeros(4900))
+    H = pg.Hamiltonian(m, params, sec)
+    with pytest.raises(pg.QcmgError) as ei:
+        H.lanczos(max_iter=3)
+    assert ei.value.code == -4
