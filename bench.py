@@ -176,7 +176,10 @@ def run_gpu(args):
         m.new_operator(name, typ, els)
     H = pg.Hamiltonian(m, PARAMS, SECTOR)
     D = H.dim
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: torch's legacy default stream has handle 0, which
+    # the engine would read as "use your own stream"
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     H.set_stream(stream.cuda_stream)
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
     x = torch.randn(D, dtype=torch.float64, device="cuda", generator=g)
@@ -202,6 +205,9 @@ def run_gpu(args):
         torch.cuda.synchronize()
     if world > 1:
         torch.distributed.barrier()
+    y_sum = float(torch.sum(torch.abs(y)).item())  # surfaces any asynchronous fault
+    if not (y_sum > 0.0):
+        raise RuntimeError("product produced an empty result")
     total_ms = t_all0.elapsed_time(t_all1)
     per_launch = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     if world > 1:
