@@ -112,6 +112,29 @@ int qcmg_hamiltonian_halfop(const qcmg_hamiltonian* H, int spin, size_t* nnz, ui
  * and HS_interaction_operator::multiply_add (HS_interaction_operator.hpp:62-70). */
 int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags);
 
+/* Chooses the arithmetic of the handle's products and Lanczos runs:
+ * path 1 (default) uses the fixed-point fast path whenever the sector's hops
+ * have one magnitude per spin (the Hubbard form), path 0 always uses the
+ * FP64 kernels.  No counterpart in the reference (FP64 throughout). */
+int qcmg_hamiltonian_set_path(qcmg_hamiltonian* H, int path);
+
+/* *available = 1 when the fixed-point fast path applies to this sector. */
+int qcmg_hamiltonian_fx_available(qcmg_hamiltonian* H, int* available);
+
+/* Device vectors in the fixed-point format of the fast path:
+ * value_i = q_i * 2^E with |q_i| < 2^mb.  Conversions run on `stream`
+ * (a cudaStream_t, NULL = default stream); all pointers are device pointers. */
+int qcmg_fx_from_f64(size_t n, const double* x, int64_t* q, int* E, int* mb, void* stream);
+int qcmg_fx_to_f64(size_t n, const int64_t* q, int E, double* x, void* stream);
+
+/* y = H x on fixed-point device vectors (length dim): x given by (qx, Ex,
+ * mbx); the result's exponent is returned in *Ey (|qy| < 2^56).  Launches on
+ * the handle's stream; QCMG_ASYNC returns without waiting.  Same product as
+ * qcmg_matvec (Hamiltonian_Factorized::mult_add), exact integer arithmetic
+ * on the hops and one rounding per diagonal term. */
+int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int64_t* qy, int* Ey,
+                   unsigned flags);
+
 /* Seeded start vector of the reference: std::default_random_engine(seed)
  * drawing std::normal_distribution(0,1), normalized.
  * Replaces random() (src_util/vector_num.cpp:114-119). */

@@ -47,6 +47,11 @@ SIGNATURES = {
     "qcmg_hamiltonian_dims": (c_int, [vp, size_p, size_p, size_p]),
     "qcmg_hamiltonian_halfop": (c_int, [vp, c_int, size_p, vp, vp, vp, vp]),
     "qcmg_matvec": (c_int, [vp, vp, vp, c_uint]),
+    "qcmg_hamiltonian_set_path": (c_int, [vp, c_int]),
+    "qcmg_hamiltonian_fx_available": (c_int, [vp, int_p]),
+    "qcmg_fx_from_f64": (c_int, [c_size_t, vp, vp, int_p, int_p, vp]),
+    "qcmg_fx_to_f64": (c_int, [c_size_t, vp, c_int, vp, vp]),
+    "qcmg_matvec_fx": (c_int, [vp, vp, c_int, c_int, vp, int_p, c_uint]),
     "qcmg_seeded_vector": (c_int, [c_size_t, c_uint, vp]),
     "qcmg_lanczos_ground_state": (c_int, [vp, vp, c_uint, c_double, c_int, c_int, dbl_p, vp,
                                           int_p, vp, vp, c_int]),

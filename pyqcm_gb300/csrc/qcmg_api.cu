@@ -10,6 +10,7 @@
 
 #include "qcmg.h"
 #include "qcmg_internal.h"
+#include "qcmg_fxpath.h"
 #include "qcmg_krylov.h"
 
 namespace qcmg {
@@ -296,8 +297,12 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
     QCMG_CUDA(cudaSetDevice(H->device));
     const bool acc = (flags & QCMG_ACCUMULATE) != 0;
     const size_t n = H->dim;
+    const bool fx = H->use_fx && fx_prepare(H);
     if (flags & QCMG_DEVICE_PTRS) {
-      matvec(H, x, y, acc);
+      if (fx)
+        fx_matvec_f64(H, x, y, acc);
+      else
+        matvec(H, x, y, acc);
       if (!(flags & QCMG_ASYNC)) QCMG_CUDA(cudaStreamSynchronize(H->stream));
       return;
     }
@@ -305,9 +310,81 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
     H->ybuf.alloc(n);
     QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
     if (acc) QCMG_CUDA(cudaMemcpyAsync(H->ybuf.p, y, n * 8, cudaMemcpyHostToDevice, H->stream));
-    matvec(H, H->xbuf.p, H->ybuf.p, acc);
+    if (fx)
+      fx_matvec_f64(H, H->xbuf.p, H->ybuf.p, acc);
+    else
+      matvec(H, H->xbuf.p, H->ybuf.p, acc);
     QCMG_CUDA(cudaMemcpyAsync(y, H->ybuf.p, n * 8, cudaMemcpyDeviceToHost, H->stream));
     QCMG_CUDA(cudaStreamSynchronize(H->stream));
+  });
+}
+
+int qcmg_hamiltonian_set_path(qcmg_hamiltonian* H, int path) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr, "NULL handle");
+    QCMG_CHECK_ARG(path == 0 || path == 1, "path must be 0 (FP64) or 1 (fixed point)");
+    std::lock_guard<std::mutex> lock(H->mu);
+    H->use_fx = path;
+  });
+}
+
+int qcmg_hamiltonian_fx_available(qcmg_hamiltonian* H, int* available) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && available != nullptr, "NULL argument");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    *available = fx_prepare(H) ? 1 : 0;
+  });
+}
+
+int qcmg_fx_from_f64(size_t n, const double* x, int64_t* q, int* E, int* mb, void* stream) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(x && q && E && mb, "NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    FxVec v;
+    DevBuf<unsigned long long> tmp;
+    fx_from_f64(x, n, v, s, tmp);
+    if (n) QCMG_CUDA(cudaMemcpyAsync(q, v.buf.p, n * 8, cudaMemcpyDeviceToDevice, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+    *E = v.E;
+    *mb = v.mb;
+  });
+}
+
+int qcmg_fx_to_f64(size_t n, const int64_t* q, int E, double* x, void* stream) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(x && q, "NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    FxVec v;
+    v.buf.borrow(const_cast<int64_t*>(q), n);
+    v.n = n;
+    v.E = E;
+    v.c = 1.0;
+    fx_to_f64(v, x, s);
+    QCMG_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
+int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int64_t* qy, int* Ey,
+                   unsigned flags) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H && qx && qy && Ey, "NULL argument");
+    QCMG_CHECK_ARG(qx != qy, "x and y must not alias");
+    QCMG_CHECK_ARG(mbx >= 0 && mbx <= 62, "invalid bit length");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    QCMG_CHECK_ARG(fx_prepare(H), "this Hamiltonian has no fixed-point form (hop magnitudes differ)");
+    FxVec x, y;
+    x.buf.borrow(const_cast<int64_t*>(qx), H->dim);
+    x.n = H->dim;
+    x.E = Ex;
+    x.mb = mbx;
+    x.c = 1.0;
+    y.buf.borrow(qy, H->dim);
+    y.n = H->dim;
+    fx_matvec(H, x, y, nullptr, 0.0);
+    *Ey = y.E;
+    if (!(flags & QCMG_ASYNC)) QCMG_CUDA(cudaStreamSynchronize(H->stream));
   });
 }
 

@@ -1,0 +1,32 @@
+// FX64 fast path (fixed-point Krylov vectors): host-side declarations.
+#pragma once
+
+#include <cstdint>
+
+#include "qcmg_internal.h"
+#include "qcmg_krylov.h"
+
+namespace qcmg {
+
+struct I128;
+
+struct FxReducer {
+  DevBuf<I128> part;
+  DevBuf<I128> out;
+  DevBuf<unsigned long long> umax;
+  double dot(const FxVec& a, const FxVec& b, cudaStream_t s);
+};
+
+// Prepares the fixed-point tables; false if the Hamiltonian does not have
+// one hop magnitude per spin (then the FP64 path is used).
+bool fx_prepare(qcmg_hamiltonian* H);
+void fx_from_f64(const double* x, size_t n, FxVec& v, cudaStream_t s,
+                 DevBuf<unsigned long long>& tmp);
+void fx_to_f64(const FxVec& v, double* x, cudaStream_t s);
+void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma);
+// y (+)= H x on FP64 device vectors through the fixed-point product.
+void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
+LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, int max_iter,
+                         double* psi_dev);
+
+}  // namespace qcmg

@@ -39,17 +39,27 @@ template <class T>
 struct DevBuf {
   T* p = nullptr;
   size_t n = 0;
+  bool owned = true;  // false: p belongs to the caller and is never freed here
   DevBuf() = default;
   DevBuf(const DevBuf&) = delete;
   DevBuf& operator=(const DevBuf&) = delete;
   ~DevBuf() { release(); }
   void release() {
-    if (p) cudaFree(p);
+    if (p && owned) cudaFree(p);
     p = nullptr;
     n = 0;
+    owned = true;
+  }
+  // Wraps caller-owned device memory.
+  void borrow(T* ptr, size_t count) {
+    release();
+    p = ptr;
+    n = count;
+    owned = false;
   }
   void alloc(size_t count) {
     if (count <= n && p) return;
+    QCMG_CHECK_ARG(owned, "cannot grow a borrowed buffer");
     release();
     size_t bytes = (count ? count : 1) * sizeof(T);
     QCMG_CUDA(cudaMalloc(&p, bytes));
@@ -100,6 +110,35 @@ uint64_t binomial(int n, int k);
 // Interaction diagonal kinds.
 enum { QCMG_INTER_NONE = 0, QCMG_INTER_ONSITE = 1, QCMG_INTER_GENERAL = 2 };
 
+namespace qcmg {
+// Device vector of the fixed-point fast path: value_i = c * 2^E * q_i with
+// |q_i| < 2^mb.
+struct FxVec {
+  DevBuf<int64_t> buf;
+  size_t n = 0;
+  int E = 0;
+  int mb = 0;
+  double c = 1.0;
+  void alloc(size_t count);
+};
+
+// Tables of the fixed-point product (built on first use by fx_prepare).
+struct FxTables {
+  int state = 0;  // 0 not built, 1 usable, -1 not applicable
+  DevBuf<uint32_t> rp_up, rs_up, col_up, rp_dn, rs_dn, col_dn;
+  double t_up = 0.0, t_dn = 0.0;  // hop magnitude of each spin
+  int maxdeg_up = 0, maxdeg_dn = 0;
+  DevBuf<int64_t> dup, ddn, wdn;  // diagonal in units of 2^-G
+  int64_t U = 0;
+  int G = 0;
+  double bound = 0.0;  // bound on |H|_inf
+  int b = 0;
+  uint32_t band = 0;  // rows per band of the down-spin pass
+  FxVec x, y;         // staging of the FP64-interface product
+  DevBuf<unsigned long long> tmp;
+};
+}  // namespace qcmg
+
 struct qcmg_hamiltonian {
   int device = 0;
   int L = 0, nup = 0, ndn = 0;
@@ -117,7 +156,9 @@ struct qcmg_hamiltonian {
   // deterministic reduction scratch
   qcmg::DevBuf<double> partials;
   qcmg::DevBuf<double> scalars;
-  std::mutex mu;  // serializes calls on one handle
+  qcmg::FxTables fx;
+  int use_fx = 1;  // 1: fixed-point fast path when applicable; 0: FP64 kernels
+  std::mutex mu;   // serializes calls on one handle
 };
 
 namespace qcmg {

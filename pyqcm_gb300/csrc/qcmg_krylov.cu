@@ -10,6 +10,7 @@
 #include <random>
 
 #include "qcmg_blas.h"
+#include "qcmg_fxpath.h"
 #include "qcmg_internal.h"
 #include "qcmg_krylov.h"
 #include "qcmg_tridiag.h"
@@ -150,6 +151,15 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
   }
   DevVec x0(n), r(n), q(n);
   QCMG_CUDA(cudaMemcpyAsync(x0.p, x0_host, n * 8, cudaMemcpyHostToDevice, s));
+  if (reorth <= 0 && H->use_fx && fx_prepare(H)) {
+    // fixed-point fast path (one hop magnitude per spin)
+    LanczosResult fr = fx_lanczos(H, x0.p, tol, max_iter, psi_host ? r.p : nullptr);
+    if (psi_host) {
+      QCMG_CUDA(cudaMemcpyAsync(psi_host, r.p, n * 8, cudaMemcpyDeviceToHost, s));
+      QCMG_CUDA(cudaStreamSynchronize(s));
+    }
+    return fr;
+  }
   QCMG_CUDA(cudaMemcpyAsync(r.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
   QCMG_CUDA(cudaMemsetAsync(q.p, 0, n * 8, s));
   Reducer red;

@@ -184,6 +184,22 @@ class Hamiltonian:
         """Launch on a caller-owned cudaStream_t (int handle, 0 = own stream)."""
         check(lib().qcmg_hamiltonian_set_stream(self._h, stream_ptr or None))
 
+    def set_path(self, fixed_point):
+        """True: fixed-point fast path where it applies (default); False: FP64."""
+        check(lib().qcmg_hamiltonian_set_path(self._h, 1 if fixed_point else 0))
+
+    def fx_available(self):
+        a = _lib.c_int()
+        check(lib().qcmg_hamiltonian_fx_available(self._h, a))
+        return bool(a.value)
+
+    def matvec_fx_device(self, qx_ptr, Ex, mbx, qy_ptr, asynchronous=False):
+        """y = H x on fixed-point device vectors; returns the exponent of y."""
+        Ey = _lib.c_int()
+        check(lib().qcmg_matvec_fx(self._h, qx_ptr, Ex, mbx, qy_ptr, Ey,
+                                   _lib.QCMG_ASYNC if asynchronous else 0))
+        return Ey.value
+
     def halfop(self, spin):
         nnz = _lib.c_size_t()
         check(lib().qcmg_hamiltonian_halfop(self._h, spin, nnz, None, None, None, None))

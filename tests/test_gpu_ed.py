@@ -73,11 +73,13 @@ def test_matvec_matches_reference(pg, tag):
     assert np.max(np.abs(y2 - 1.0 - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("path", ["fixed_point", "fp64"])
 @pytest.mark.parametrize("tag", list(CASES))
-def test_lanczos_ground_state(pg, tag):
+def test_lanczos_ground_state(pg, tag, path):
     g = load_golden(tag)
     m, params, sec = engine_model(tag)
     H = pg.Hamiltonian(m, params, sec)
+    H.set_path(path == "fixed_point")
     e0, psi, al, be = H.lanczos()  # seeded start, as the reference's states()
     assert abs(e0 - g["lz_E0"]) <= 1e-10 * abs(g["lz_E0"])
     assert abs(len(al) - len(g["lz_alpha"])) <= 2
@@ -171,3 +173,79 @@ def test_errors(pg):
     with pytest.raises(pg.QcmgError) as ei:
         H.lanczos(max_iter=3)
     assert ei.value.code == -4
+
+
+@pytest.mark.parametrize("tag", ["chain8", "chain8_n7"])
+def test_fixed_point_product_matches_reference(pg, tag):
+    """The fixed-point product (hops +-t) against the reference's FP64 product."""
+    g = load_golden(tag)
+    m, params, sec = engine_model(tag)
+    H = pg.Hamiltonian(m, params, sec)
+    assert H.fx_available()
+    x = g["h_x0"]
+    ref = g["h_Hx0"]
+    y = H.matvec(x)
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+    y2 = np.full(H.dim, 0.25)
+    H.mult_add(x, y2)
+    assert np.max(np.abs(y2 - 0.25 - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
+def test_fixed_point_not_used_for_mixed_hops(pg):
+    m, params, sec = engine_model("ladder2x4_af")  # t and t' differ
+    H = pg.Hamiltonian(m, params, sec)
+    assert not H.fx_available()
+
+
+def _torch():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def test_fixed_point_conversion_roundtrip(pg):
+    torch = _torch()
+    from pyqcm_gb300 import _lib
+    x = torch.randn(100003, dtype=torch.float64, device="cuda") * 1e-3
+    x[7] = 0.0
+    q = torch.empty(x.numel(), dtype=torch.int64, device="cuda")
+    E, mb = _lib.c_int(), _lib.c_int()
+    _lib.check(pg.lib().qcmg_fx_from_f64(x.numel(), x.data_ptr(), q.data_ptr(), E, mb, None))
+    back = torch.empty_like(x)
+    _lib.check(pg.lib().qcmg_fx_to_f64(x.numel(), q.data_ptr(), E.value, back.data_ptr(), None))
+    err = float((back - x).abs().max())
+    assert err <= 2.0 ** (E.value - 1) * 1.0000001
+    assert err <= 2.0 ** -55 * float(x.abs().max())
+    assert float(back[7]) == 0.0
+
+
+def test_fixed_point_product_4x4_full_sector(pg):
+    """4x4 Hubbard cluster, half filling (dim 165,636,900): fixed-point
+    product against the FP64 product, both on the GPU, same vector."""
+    torch = _torch()
+    import models
+    from pyqcm_gb300 import _lib
+    ns, nb, ops = models.hubbard_cluster(4, 4)
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, {"t": 1.0, "U": 8.0, "mu": 4.0}, "R0:N16:S0")
+    assert H.dim == 165636900 and H.fx_available()
+    gen = torch.Generator(device="cuda").manual_seed(7)
+    x = torch.randn(H.dim, dtype=torch.float64, device="cuda", generator=gen)
+    x /= torch.linalg.vector_norm(x)
+    qx = torch.empty(H.dim, dtype=torch.int64, device="cuda")
+    E, mb = _lib.c_int(), _lib.c_int()
+    _lib.check(pg.lib().qcmg_fx_from_f64(H.dim, x.data_ptr(), qx.data_ptr(), E, mb, None))
+    qy = torch.empty_like(qx)
+    Ey = H.matvec_fx_device(qx.data_ptr(), E.value, mb.value, qy.data_ptr())
+    y_fx = torch.empty_like(x)
+    _lib.check(pg.lib().qcmg_fx_to_f64(H.dim, qy.data_ptr(), Ey, y_fx.data_ptr(), None))
+    H.set_path(False)
+    y64 = torch.empty_like(x)
+    H.matvec_device(x.data_ptr(), y64.data_ptr())
+    err = float((y_fx - y64).abs().max())
+    assert err <= 1e-13 * float(y64.abs().max())
+    del qx, qy, y_fx, y64, x
+    torch.cuda.empty_cache()
