@@ -31,15 +31,20 @@ METRIC = "lanczos_hpsi_gbs"
 UNIT = "GB/s"
 NX, NY = 4, 4
 PARAMS = {"t": 1.0, "U": 8.0, "mu": 4.0}
-SECTOR = "R0:N16:S0"
 BYTES_PER_STATE = 24
 
 
-def workload_config():
-    return {"workload": "4x4 Hubbard cluster, t=1 U=8 mu=4, sector N=16 Sz=0 "
-                        "(dim 165,636,900), y = H x FP64",
-            "dim": 165636900, "bytes_per_step": BYTES_PER_STATE * 165636900,
-            "l2": "inputs larger than L2 (2 x 1.33 GB)", "parallelism": "replicas"}
+def sector_of(nx, ny):
+    n = nx * ny
+    return f"R0:N{n}:S{n % 2}", (n + n % 2) // 2, n // 2
+
+
+def workload_config(dim=165636900):
+    sec = sector_of(NX, NY)[0]
+    return {"workload": f"{NX}x{NY} Hubbard cluster, t=1 U=8 mu=4, sector {sec} "
+                        f"(dim {dim:,}), y = H x",
+            "dim": dim, "bytes_per_step": BYTES_PER_STATE * dim,
+            "l2": "inputs larger than L2", "parallelism": "replicas"}
 
 
 def model_ops():
@@ -130,7 +135,8 @@ def cpu_port_timing(steps, threads):
     import qcm_oracle as qo
     ns, nb, ops = model_ops()
     up, dn, pr = qo.combine_terms(ops, PARAMS, ns)
-    S = qo.Sector(ns, 8, 8, up, dn, pr)
+    _, nup, ndn = sector_of(NX, NY)
+    S = qo.Sector(ns, nup, ndn, up, dn, pr)
     x = np.random.default_rng(1).standard_normal(S.dim)
     x /= np.linalg.norm(x)
     y = np.zeros(S.dim)
@@ -174,7 +180,7 @@ def run_gpu(args):
     m = pg.ClusterModel(ns, nb)
     for name, (typ, els) in ops.items():
         m.new_operator(name, typ, els)
-    H = pg.Hamiltonian(m, PARAMS, SECTOR)
+    H = pg.Hamiltonian(m, PARAMS, sector_of(NX, NY)[0])
     D = H.dim
     # a dedicated stream: torch's legacy default stream has handle 0, which
     # the engine would read as "use your own stream"
@@ -253,7 +259,7 @@ def run_gpu(args):
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int64" if fast else "f64",
-            "data": "synthetic", "config": workload_config(),
+            "data": "synthetic", "config": workload_config(D),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": UNIT,
                          "frac": achieved / peak, "traffic": profile_traffic(),
                          "peak_kind": peak_kind, "kernels": kernels},
@@ -280,7 +286,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="qcmg", choices=["qcmg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cluster", default="4x4",
+                    help="NXxNY Hubbard cluster at half filling (profiling of smaller cases)")
     args = ap.parse_args()
+    global NX, NY
+    NX, NY = (int(v) for v in args.cluster.split("x"))
     if args.impl == "reference":
         run_reference(args)
     else:

@@ -19,6 +19,24 @@
 //   hyb LABEL SPIN RE IM TAG                  -> ED::hybridization_function(z)
 //   sigma LABEL SPIN RE IM TAG                -> ED::self_energy(z)
 //   omega LABEL TAG                           -> ED::Potthoff_functional (cluster part)
+// Lattice (QCM) commands, mirroring the pyqcm Python calls:
+//   lat_cluster MODEL x y z [x y z ...]       -> QCM::add_cluster + QCM::add_system
+//   lat_model NAME a1x a1y a1z [a2x a2y a2z]  -> QCM::new_lattice_model (unit cell = identity)
+//   lat_hop NAME lx ly lz AMP TAU SIGMA       -> QCM::hopping_operator
+//   lat_inter NAME AMP TYPE                   -> QCM::interaction_operator (on-site)
+//   lat_dw NAME TYPE Qx Qy Qz AMP PHASE       -> QCM::density_wave
+//   lat_param NAME VALUE | lat_equiv NAME MULT REF
+//   lat_sector S                              -> target sector of the system
+//   lat_instance LABEL                        -> QCM::set_parameters + new_model_instance
+//   lat_kgrid NX NY NZ                        -> QCM::set_wavevector_grid
+//   lat_wgrid N w_1..w_N p_1..p_N             -> discrete frequency grid
+//   lat_sef LABEL TAG                         -> QCM::Potthoff_functional
+//   lat_gper LABEL TAG NZ (re im)x NZ NK (kx ky kz)x NK -> periodized_Green_function
+//   lat_tk LABEL TAG NK (kx ky kz)x NK        -> QCM::tk
+//   lat_dump LABEL TAG                        -> neighbours, inter-cluster elements, H, Hc
+//   lat_varia NAME...                         -> QCM::CDMFT_variational_set (cluster 0)
+//   lat_host LABEL TAG NW w.. wt..            -> QCM::CDMFT_host (+ get_CDMFT_host)
+//   lat_dist LABEL TAG NP p..                 -> QCM::CDMFT_distance (cluster 0)
 #include <complex>
 #include <cstdio>
 #include <fstream>
@@ -31,6 +49,7 @@
 
 #include "QCM.hpp"
 #include "lattice_model.hpp"
+#include "lattice_model_instance.hpp"
 #include "global_parameter.hpp"
 #include "model_instance.hpp"
 #include "qcm_ED.hpp"
@@ -44,6 +63,9 @@ extern map<string, shared_ptr<model>> models;
 extern map<size_t, shared_ptr<model_instance_base>> model_instances;
 extern std::normal_distribution<double> normal_dis;
 extern shared_ptr<lattice_model> qcm_model;
+extern map<int, unique_ptr<lattice_model_instance>> lattice_model_instances;
+extern vector<double> grid_freqs;
+extern vector<double> grid_weights;
 
 static string outdir = ".";
 static ofstream manifest;
@@ -78,6 +100,9 @@ struct Spec {
   map<string, map<string, string>> optype;
   map<string, double> params;
   set<string> ops_created;
+  vector<pair<string, double>> lat_values;
+  vector<tuple<string, double, string>> lat_equiv;
+  bool lat_params_set = false;
 };
 
 static void create_ops(Spec& S, const string& model) {
@@ -245,6 +270,134 @@ int main(int argc, char** argv) {
         size_t label; string tag; ss >> label >> tag;
         ED::Green_function_solve(label);
         put_scalar(tag, ED::Potthoff_functional(label));
+      } else if (cmd == "lat_cluster") {
+        string m; ss >> m;
+        vector<vector3D<int64_t>> pos;
+        int64_t x, y, z;
+        while (ss >> x >> y >> z) pos.push_back(vector3D<int64_t>(x, y, z));
+        QCM::add_cluster(vector3D<int64_t>(0, 0, 0), pos, -1, false);
+        QCM::add_system(m, 0);
+      } else if (cmd == "lat_model") {
+        string name; ss >> name;
+        vector<int64_t> sl;
+        int64_t v;
+        while (ss >> v) sl.push_back(v);
+        vector<int64_t> uc(sl.size(), 0);
+        for (size_t i = 0; i < sl.size() / 3; i++) uc[i * 4] = 1;
+        QCM::new_lattice_model(name, sl, uc);
+      } else if (cmd == "lat_hop") {
+        string name; int64_t x, y, z; double amp; int tau, sigma;
+        ss >> name >> x >> y >> z >> amp >> tau >> sigma;
+        vector3D<int64_t> lk(x, y, z);
+        QCM::hopping_operator(name, lk, amp, 1, 1, tau, sigma);
+      } else if (cmd == "lat_inter") {
+        string name, type; double amp; ss >> name >> amp >> type;
+        vector3D<int64_t> lk(0, 0, 0);
+        QCM::interaction_operator(name, lk, amp, 1, 1, type);
+      } else if (cmd == "lat_dw") {
+        string name, type; double qx, qy, qz, amp, phase;
+        ss >> name >> type >> qx >> qy >> qz >> amp >> phase;
+        vector3D<int64_t> lk(0, 0, 0);
+        QCM::density_wave(name, lk, complex<double>(amp), 0, vector3D<double>(qx, qy, qz), phase, type);
+      } else if (cmd == "lat_param") {
+        string n; double v; ss >> n >> v; S.lat_values.push_back({n, v});
+      } else if (cmd == "lat_equiv") {
+        string n, r; double m; ss >> n >> m >> r; S.lat_equiv.push_back(make_tuple(n, m, r));
+      } else if (cmd == "lat_sector") {
+        string sec; ss >> sec; qcm_model->sector_strings.assign(1, sec);
+      } else if (cmd == "lat_instance") {
+        int label; ss >> label;
+        if (!S.lat_params_set) {
+          QCM::set_parameters(S.lat_values, S.lat_equiv);
+          S.lat_params_set = true;
+        } else {
+          for (auto& p : S.lat_values) QCM::set_parameter(p.first, p.second);
+        }
+        QCM::new_model_instance(label);
+      } else if (cmd == "lat_set") {
+        string n; double v; ss >> n >> v;
+        for (auto& p : S.lat_values) if (p.first == n) p.second = v;
+        QCM::set_parameter(n, v);
+      } else if (cmd == "lat_kgrid") {
+        int a, b, c; ss >> a >> b >> c; QCM::set_wavevector_grid(a, b, c);
+      } else if (cmd == "lat_wgrid") {
+        int n; ss >> n;
+        grid_freqs.resize(n); grid_weights.resize(n);
+        for (int i = 0; i < n; i++) ss >> grid_freqs[i];
+        for (int i = 0; i < n; i++) ss >> grid_weights[i];
+      } else if (cmd == "lat_sef") {
+        int label; string tag; ss >> label >> tag;
+        put_scalar(tag, QCM::Potthoff_functional(label));
+      } else if (cmd == "lat_gper" || cmd == "lat_tk") {
+        int label; string tag; ss >> label >> tag;
+        vector<cplx> zs;
+        if (cmd == "lat_gper") {
+          int nz; ss >> nz;
+          for (int i = 0; i < nz; i++) { double re, im; ss >> re >> im; zs.push_back(cplx(re, im)); }
+        }
+        int nk; ss >> nk;
+        vector<vector3D<double>> ks;
+        for (int i = 0; i < nk; i++) { double a, b, c; ss >> a >> b >> c; ks.push_back(vector3D<double>(a, b, c)); }
+        vector<cplx> out;
+        size_t d = 0;
+        if (cmd == "lat_gper") {
+          for (auto z : zs) {
+            auto G = QCM::periodized_Green_function(z, ks, false, label);
+            for (auto& g : G) { d = g.r; for (size_t i = 0; i < g.r; i++) for (size_t j = 0; j < g.c; j++) out.push_back(g(i, j)); }
+          }
+          put(tag, "c16", {zs.size(), ks.size(), d, d}, out.data(), out.size());
+        } else {
+          auto T = QCM::tk(ks, false, label);
+          for (auto& g : T) { d = g.r; for (size_t i = 0; i < g.r; i++) for (size_t j = 0; j < g.c; j++) out.push_back(g(i, j)); }
+          put(tag, "c16", {ks.size(), d, d}, out.data(), out.size());
+        }
+      } else if (cmd == "lat_dump") {
+        int label; string tag; ss >> label >> tag;
+        auto& I = *lattice_model_instances.at(label);
+        auto& M = *qcm_model;
+        vector<double> nb;
+        for (auto& n : M.neighbor) { nb.push_back(n.x); nb.push_back(n.y); nb.push_back(n.z); }
+        put(tag + "_neighbors", "f8", {M.neighbor.size(), 3}, nb.data(), nb.size());
+        vector<double> gp;
+        for (auto& p : M.Green_to_position) { gp.push_back(p.x); gp.push_back(p.y); gp.push_back(p.z); }
+        put(tag + "_gpos", "f8", {M.Green_to_position.size(), 3}, gp.data(), gp.size());
+        vector<double> el;  // r, c, n, re, im (parameter value applied)
+        for (auto& op : M.term) {
+          auto it = I.params.find(op.second->name);
+          if (it == I.params.end()) continue;
+          for (auto& e : op.second->IGF_elem) {
+            cplx v = e.v * it->second;
+            el.insert(el.end(), {(double)e.r, (double)e.c, (double)e.n, v.real(), v.imag()});
+          }
+        }
+        put(tag + "_igf", "f8", {el.size() / 5, 5}, el.data(), el.size());
+        put_cmat(tag + "_H", I.H);
+        matrix<cplx> Hc = I.Hc.build_matrix();
+        put_cmat(tag + "_Hc", Hc);
+        vector<double> sd;
+        for (int i = 0; i < 3; i++) { vector3D<double> e(i == 0, i == 1, i == 2); auto v = M.superdual.to(M.physdual.from(e)); sd.push_back(v.x); sd.push_back(v.y); sd.push_back(v.z); }
+        put(tag + "_kmap", "f8", {3, 3}, sd.data(), sd.size());
+      } else if (cmd == "lat_varia") {
+        vector<string> names; string n;
+        while (ss >> n) names.push_back(n);
+        vector<vector<string>> v(1, names);
+        QCM::CDMFT_variational_set(v);
+      } else if (cmd == "lat_host") {
+        int label; string tag; int nw; ss >> label >> tag >> nw;
+        vector<double> w(nw), wt(nw);
+        for (int i = 0; i < nw; i++) ss >> w[i];
+        for (int i = 0; i < nw; i++) ss >> wt[i];
+        QCM::CDMFT_host(w, wt, label);
+        auto Hh = QCM::get_CDMFT_host(false, label);
+        vector<cplx> out;
+        size_t d = 0;
+        for (auto& row : Hh) for (auto& g : row) { d = g.r; for (size_t i = 0; i < g.r; i++) for (size_t j = 0; j < g.c; j++) out.push_back(g(i, j)); }
+        put(tag, "c16", {(size_t)nw, d, d}, out.data(), out.size());
+      } else if (cmd == "lat_dist") {
+        int label; string tag; int np; ss >> label >> tag >> np;
+        vector<double> p(np);
+        for (int i = 0; i < np; i++) ss >> p[i];
+        put_scalar(tag, QCM::CDMFT_distance(p, 0, label));
       } else {
         throw runtime_error("unknown spec command: " + cmd);
       }

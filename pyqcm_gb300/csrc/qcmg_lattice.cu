@@ -1,0 +1,469 @@
+// k x omega lattice integrals over the Lehmann cluster Green function
+// (CPT / VCA / CDMFT), batched on the GPU in FP64.
+//
+// Inputs (one spin block): the cluster Green function G(z) from its
+// Q-matrix (e, v), the bath hybridization Gamma(z) = tcb diag(1/(z-eb)) tcb^+,
+// and the lattice hopping in Fourier form
+//   t(K) - t_c = Hdiff + sum_e v_e exp(2 pi i K.R_{n_e}) |r_e><c_e|
+// with K in the reduced (superlattice-dual) basis, as the reference builds it
+// (lattice_model_instance::set_V, src_qcm/CPT.cpp:22-64).  Then
+//   V(K,z) = t(K) - t_c - Gamma(z),
+// and every per-(K,z) quantity goes through M(K,z) = G(z)^-1 - V(K,z):
+//   SEF   log|det(V G - 1)| = log|det M| + log|det G|        (lattice_model_instance.cpp:624-643)
+//   CPT   Gcpt = G (1 - V G)^-1 = M^-1                       (CPT.cpp:76-86)
+//         g(K) = (1/L) sum_ab Gcpt_ab e^{2 pi i K.(x_b - x_a)} (lattice_model.cpp:724-740)
+//   CDMFT PGF(z) = mean_K Gcpt(K, z)                          (CPT.cpp:283-345)
+// G^-1 and log|det G| are computed once per frequency; each (K, z) point then
+// costs one LU factorization of an L x L complex matrix, done by one thread
+// with its matrix in shared memory (interleaved across threads, no bank
+// conflicts).
+#include <cmath>
+#include <vector>
+
+#include "qcmg_internal.h"
+#include "qcmg_krylov.h"
+#include "qcmg_lattice.h"
+
+namespace qcmg {
+
+struct cdbl {
+  double x, y;
+};
+__device__ __forceinline__ cdbl cmul(cdbl a, cdbl b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+__device__ __forceinline__ cdbl cfma_sub(cdbl acc, cdbl a, cdbl b) {  // acc - a*b
+  return {acc.x - (a.x * b.x - a.y * b.y), acc.y - (a.x * b.y + a.y * b.x)};
+}
+__device__ __forceinline__ cdbl cinv(cdbl a) {
+  double d = a.x * a.x + a.y * a.y;
+  return {a.x / d, -a.y / d};
+}
+
+// ---------------------------------------------------------------------------
+// Per-frequency preparation: Base(z) = G(z)^-1 + Gamma(z) - Hdiff and
+// log|det G(z)|, one block per frequency, Gauss-Jordan with partial pivoting
+// in shared memory.
+
+__global__ void k_freq_prep(int L, int nw, const double2* __restrict__ G,  // nw x L x L (G[b + a L] = G(b,a))
+                            const double2* __restrict__ z, int nb, const double2* __restrict__ tcb,
+                            const double* __restrict__ eb, const double2* __restrict__ Hdiff,
+                            double2* __restrict__ base, double* __restrict__ logdetG) {
+  extern __shared__ double2 sm[];
+  double2* A = sm;              // L x 2L augmented [G | I], row-major A[r*2L + c]
+  __shared__ int piv;
+  __shared__ double ldet;
+  const int w = blockIdx.x;
+  const int L2 = 2 * L;
+  // G(r, c) with numpy orientation: G stored as G[b + a L] = G(b, a)  ->  G(r,c) = Gw[r + c L]
+  const double2* Gw = G + (size_t)w * L * L;
+  for (int idx = threadIdx.x; idx < L * L2; idx += blockDim.x) {
+    int r = idx / L2, c = idx % L2;
+    A[idx] = c < L ? Gw[r + c * L] : make_double2(c - L == r ? 1.0 : 0.0, 0.0);
+  }
+  if (threadIdx.x == 0) ldet = 0.0;
+  __syncthreads();
+  for (int p = 0; p < L; ++p) {
+    if (threadIdx.x == 0) {
+      int best = p;
+      double bv = -1.0;
+      for (int r = p; r < L; ++r) {
+        double2 a = A[r * L2 + p];
+        double m = a.x * a.x + a.y * a.y;
+        if (m > bv) {
+          bv = m;
+          best = r;
+        }
+      }
+      piv = best;
+      ldet += 0.5 * log(bv);
+    }
+    __syncthreads();
+    if (piv != p)
+      for (int c = threadIdx.x; c < L2; c += blockDim.x) {
+        double2 t = A[p * L2 + c];
+        A[p * L2 + c] = A[piv * L2 + c];
+        A[piv * L2 + c] = t;
+      }
+    __syncthreads();
+    const double2 pp = A[p * L2 + p];
+    const cdbl ip = cinv({pp.x, pp.y});
+    __syncthreads();
+    for (int c = threadIdx.x; c < L2; c += blockDim.x) {
+      cdbl v = cmul({A[p * L2 + c].x, A[p * L2 + c].y}, ip);
+      A[p * L2 + c] = make_double2(v.x, v.y);
+    }
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < L * L2; idx += blockDim.x) {
+      int r = idx / L2, c = idx % L2;
+      if (r == p) continue;
+      double2 f = A[r * L2 + p];
+      double2 a = A[p * L2 + c];
+      if (c == p) continue;  // column p is cleared below
+      cdbl v = cfma_sub({A[idx].x, A[idx].y}, {f.x, f.y}, {a.x, a.y});
+      A[idx] = make_double2(v.x, v.y);
+    }
+    __syncthreads();
+    for (int r = threadIdx.x; r < L; r += blockDim.x)
+      if (r != p) A[r * L2 + p] = make_double2(0.0, 0.0);
+    __syncthreads();
+  }
+  // Base = G^-1 + Gamma - Hdiff, row-major base[r*L + c]
+  const double2 zw = z[w];
+  double2* B = base + (size_t)w * L * L;
+  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+    int r = idx / L, c = idx % L;
+    double2 gi = A[r * L2 + L + c];
+    double gx = gi.x - Hdiff[idx].x, gy = gi.y - Hdiff[idx].y;
+    for (int i = 0; i < nb; ++i) {
+      // Gamma(r,c) += tcb(r,i) conj(tcb(c,i)) / (z - eb_i)
+      double2 a = tcb[r + (size_t)L * i], b = tcb[c + (size_t)L * i];
+      double re = zw.x - eb[i], im = zw.y, den = re * re + im * im;
+      double ur = re / den, ui = -im / den;
+      double pr = a.x * b.x + a.y * b.y, pi = a.y * b.x - a.x * b.y;  // a conj(b)
+      gx += pr * ur - pi * ui;
+      gy += pr * ui + pi * ur;
+    }
+    B[idx] = make_double2(gx, gy);
+  }
+  if (threadIdx.x == 0) logdetG[w] = -ldet;  // log|det G| = -log|det G^-1|... (see below)
+}
+
+// ---------------------------------------------------------------------------
+// Per-point kernel.  MODE 0: SEF (sum of log|det M| weighted), MODE 1: CPT
+// periodized g(K,z), MODE 2: mean of M^-1 (CDMFT projected GF).
+
+struct PointArgs {
+  int L;
+  int nw;
+  const double2* base;  // nw x L x L row-major
+  int nel;
+  const int* el_r;
+  const int* el_c;
+  const int* el_n;
+  const double2* el_v;
+  int nR;
+  const double* R;  // nR x 3
+  // K points: explicit list or a grid
+  int nk;
+  const double* K;  // nk x 3 (explicit) or null
+  int gx, gy, gz;   // grid sizes (K = (i+off)/gx, ...)
+  double off;       // 0 for the SEF grid, 0.5 for the CDMFT midpoint grid
+  const double* gpos;  // L x 3 (CPT)
+  double2* out;        // MODE 1: nw x nk;  MODE 2: partial sums
+  double* part;        // MODE 0: partial sums per block
+};
+
+__device__ __forceinline__ void point_K(const PointArgs& A, int ik, double* K) {
+  if (A.K) {
+    K[0] = A.K[3 * ik];
+    K[1] = A.K[3 * ik + 1];
+    K[2] = A.K[3 * ik + 2];
+  } else {
+    int i = ik % A.gx, j = (ik / A.gx) % A.gy, l = ik / (A.gx * A.gy);
+    K[0] = (i + A.off) / A.gx;
+    K[1] = A.gy > 1 ? (j + A.off) / A.gy : 0.0;
+    K[2] = A.gz > 1 ? (l + A.off) / A.gz : 0.0;
+  }
+}
+
+template <int MODE>
+__global__ void k_points(PointArgs A) {
+  extern __shared__ double smem[];
+  const int T = blockDim.x, t = threadIdx.x, L = A.L, LL = L * L;
+  double* mr = smem;            // LL x T
+  double* mi = smem + LL * T;   // LL x T
+#define MR(r, c) mr[((r) * L + (c)) * T + t]
+#define MI(r, c) mi[((r) * L + (c)) * T + t]
+  const size_t npts = (size_t)A.nk * A.nw;
+  double acc = 0.0;
+  for (size_t pt = blockIdx.x * (size_t)T + t; pt < npts + 0 * T; pt += (size_t)gridDim.x * T) {
+    const int w = (int)(pt / A.nk), ik = (int)(pt % A.nk);
+    double K[3];
+    point_K(A, ik, K);
+    const double2* B = A.base + (size_t)w * LL;
+    for (int e = 0; e < LL; ++e) {
+      double2 b = B[e];
+      mr[e * T + t] = b.x;
+      mi[e * T + t] = b.y;
+    }
+    for (int e = 0; e < A.nel; ++e) {
+      const double* Rn = A.R + 3 * A.el_n[e];
+      double ph = 2.0 * M_PI * (K[0] * Rn[0] + K[1] * Rn[1] + K[2] * Rn[2]);
+      double s, c;
+      sincos(ph, &s, &c);
+      double2 v = A.el_v[e];
+      // M = Base - v e^{i ph} at (r, c)
+      int r = A.el_r[e], cc = A.el_c[e];
+      MR(r, cc) -= v.x * c - v.y * s;
+      MI(r, cc) -= v.x * s + v.y * c;
+    }
+    // LU with partial pivoting (row interchanges), in place.
+    int perm[32];
+    for (int i = 0; i < L; ++i) perm[i] = i;
+    double logabs = 0.0;
+    for (int p = 0; p < L; ++p) {
+      int best = p;
+      double bv = MR(p, p) * MR(p, p) + MI(p, p) * MI(p, p);
+      for (int r = p + 1; r < L; ++r) {
+        double m = MR(r, p) * MR(r, p) + MI(r, p) * MI(r, p);
+        if (m > bv) {
+          bv = m;
+          best = r;
+        }
+      }
+      if (best != p) {
+        for (int c = 0; c < L; ++c) {
+          double a = MR(p, c), b = MI(p, c);
+          MR(p, c) = MR(best, c);
+          MI(p, c) = MI(best, c);
+          MR(best, c) = a;
+          MI(best, c) = b;
+        }
+        int tp = perm[p];
+        perm[p] = perm[best];
+        perm[best] = tp;
+      }
+      logabs += 0.5 * log(bv);
+      const cdbl ip = cinv({MR(p, p), MI(p, p)});
+      for (int r = p + 1; r < L; ++r) {
+        cdbl f = cmul({MR(r, p), MI(r, p)}, ip);
+        MR(r, p) = f.x;
+        MI(r, p) = f.y;
+        for (int c = p + 1; c < L; ++c) {
+          cdbl v = cfma_sub({MR(r, c), MI(r, c)}, f, {MR(p, c), MI(p, c)});
+          MR(r, c) = v.x;
+          MI(r, c) = v.y;
+        }
+      }
+    }
+    if (MODE == 0) {
+      acc += logabs;  // weighted and combined with log|det G| by the reduction
+      (void)perm;
+    } else if (MODE == 1) {
+      // y = M^-1 u, u_b = e^{2 pi i K.x_b};  g = (1/L) u^+ y
+      cdbl y[32];
+      for (int i = 0; i < L; ++i) {
+        const double* x = A.gpos + 3 * perm[i];
+        double ph = 2.0 * M_PI * (K[0] * x[0] + K[1] * x[1] + K[2] * x[2]);
+        double s, c;
+        sincos(ph, &s, &c);
+        y[i] = {c, s};  // (P u)_i
+      }
+      for (int i = 0; i < L; ++i)  // forward: unit lower
+        for (int j = 0; j < i; ++j) y[i] = cfma_sub(y[i], {MR(i, j), MI(i, j)}, y[j]);
+      for (int i = L - 1; i >= 0; --i) {  // backward: upper
+        for (int j = i + 1; j < L; ++j) y[i] = cfma_sub(y[i], {MR(i, j), MI(i, j)}, y[j]);
+        y[i] = cmul(y[i], cinv({MR(i, i), MI(i, i)}));
+      }
+      double gr = 0.0, gi = 0.0;
+      for (int b = 0; b < L; ++b) {
+        const double* x = A.gpos + 3 * b;
+        double ph = 2.0 * M_PI * (K[0] * x[0] + K[1] * x[1] + K[2] * x[2]);
+        double s, c;
+        sincos(ph, &s, &c);
+        // conj(u_b) y_b
+        gr += c * y[b].x + s * y[b].y;
+        gi += c * y[b].y - s * y[b].x;
+      }
+      A.out[(size_t)w * A.nk + ik] = make_double2(gr / L, gi / L);
+    } else {
+      // column j of M^-1: solve M x = e_j (P applied), accumulate into out
+      double2* O = A.out + ((size_t)blockIdx.x * A.nw + w) * LL;  // unused layout guard
+      (void)O;
+      for (int j = 0; j < L; ++j) {
+        cdbl y[32];
+        for (int i = 0; i < L; ++i) y[i] = {perm[i] == j ? 1.0 : 0.0, 0.0};
+        for (int i = 0; i < L; ++i)
+          for (int q = 0; q < i; ++q) y[i] = cfma_sub(y[i], {MR(i, q), MI(i, q)}, y[q]);
+        for (int i = L - 1; i >= 0; --i) {
+          for (int q = i + 1; q < L; ++q) y[i] = cfma_sub(y[i], {MR(i, q), MI(i, q)}, y[q]);
+          y[i] = cmul(y[i], cinv({MR(i, i), MI(i, i)}));
+        }
+        // accumulate column j of the inverse: out[(w*nk + ik) ...] reduced later
+        for (int i = 0; i < L; ++i)
+          A.out[((size_t)w * A.nk + ik) * LL + i * L + j] = make_double2(y[i].x, y[i].y);
+      }
+    }
+  }
+  if (MODE == 0) {
+    // block reduction of the log sums, fixed order
+    __shared__ double red[1024];
+    red[t] = acc;
+    __syncthreads();
+    if (t == 0) {
+      double s = 0.0;
+      for (int i = 0; i < T; ++i) s += red[i];
+      A.part[blockIdx.x] = s;
+    }
+  }
+#undef MR
+#undef MI
+}
+
+// ---------------------------------------------------------------------------
+// host side
+
+static int point_threads(int L) {
+  const size_t per = (size_t)2 * L * L * 8;  // bytes per point
+  int T = (int)((180 * 1024) / per);
+  T = (T / 32) * 32;
+  if (T > 256) T = 256;
+  if (T < 32) T = 32;
+  return T;
+}
+
+void Lattice::prepare(int nw, const double* z, cudaStream_t s) {
+  QCMG_CHECK_ARG(L > 0 && L <= 32, "lattice Green function dimension must be 1..32");
+  QCMG_CHECK_ARG(M >= 0, "Q-matrix not set");
+  DevBuf<double> dz;
+  dz.upload(z, (size_t)2 * nw, s);
+  DevBuf<double> G;
+  G.alloc((size_t)2 * L * L * nw);
+  if (M > 0) {
+    green_function_batch(L, M, e.p, v.p, nw, dz.p, G.p, s);
+  } else {
+    QCMG_CUDA(cudaMemsetAsync(G.p, 0, G.n * 8, s));
+  }
+  base.alloc((size_t)2 * L * L * nw);
+  logdetG.alloc(nw);
+  size_t smem = (size_t)L * 2 * L * sizeof(double2);
+  k_freq_prep<<<nw, 128, smem, s>>>(L, nw, (const double2*)G.p, (const double2*)dz.p, nb,
+                                    (const double2*)tcb.p, eb.p, (const double2*)hdiff.p,
+                                    (double2*)base.p, logdetG.p);
+  QCMG_CUDA(cudaGetLastError());
+  QCMG_CUDA(cudaStreamSynchronize(s));
+  prepared_nw = nw;
+}
+
+static PointArgs point_args(const Lattice& lat, int nw) {
+  PointArgs A;
+  A.L = lat.L;
+  A.nw = nw;
+  A.base = (const double2*)lat.base.p;
+  A.nel = lat.nel;
+  A.el_r = lat.el_r.p;
+  A.el_c = lat.el_c.p;
+  A.el_n = lat.el_n.p;
+  A.el_v = (const double2*)lat.el_v.p;
+  A.nR = lat.nR;
+  A.R = lat.R.p;
+  A.K = nullptr;
+  A.gx = A.gy = A.gz = 1;
+  A.off = 0.0;
+  A.gpos = lat.gpos.p;
+  A.out = nullptr;
+  A.part = nullptr;
+  return A;
+}
+
+double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int nky, int nkz,
+                         cudaStream_t s) {
+  std::vector<double> z(2 * nw);
+  for (int i = 0; i < nw; ++i) {
+    z[2 * i] = 0.0;
+    z[2 * i + 1] = w[i];
+  }
+  double total = 0.0;
+  const int nk = nkx * nky * nkz;
+  // frequencies are processed one by one so the per-frequency weight is
+  // applied exactly; each launch covers the whole K grid
+  prepare(nw, z.data(), s);
+  std::vector<double> ldg(nw);
+  QCMG_CUDA(cudaMemcpyAsync(ldg.data(), logdetG.p, nw * 8, cudaMemcpyDeviceToHost, s));
+  const int T = point_threads(L);
+  const size_t smem = (size_t)2 * L * L * T * 8;
+  QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  DevBuf<double> part;
+  for (int i = 0; i < nw; ++i) {
+    PointArgs A = point_args(*this, 1);
+    A.base = (const double2*)base.p + (size_t)i * L * L;
+    A.nk = nk;
+    A.gx = nkx;
+    A.gy = nky;
+    A.gz = nkz;
+    A.off = 0.0;
+    unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
+    part.alloc(g);
+    A.part = part.p;
+    k_points<0><<<g, T, smem, s>>>(A);
+    QCMG_CUDA(cudaGetLastError());
+    std::vector<double> hp(g);
+    QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, g * 8, cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+    double sk = 0.0;
+    for (double v : hp) sk += v;
+    // log|det(VG - 1)| = log|det M| + log|det G|
+    total += wt[i] * (sk / nk + ldg[i]);
+  }
+  return total;
+}
+
+void Lattice::cpt(int nz, const double* z, int nk, const double* K, double* g, cudaStream_t s) {
+  prepare(nz, z, s);
+  PointArgs A = point_args(*this, nz);
+  DevBuf<double> dK, out;
+  dK.upload(K, (size_t)3 * nk, s);
+  out.alloc((size_t)2 * nz * nk);
+  A.nk = nk;
+  A.K = dK.p;
+  A.out = (double2*)out.p;
+  const int T = point_threads(L);
+  const size_t smem = (size_t)2 * L * L * T * 8;
+  QCMG_CUDA(cudaFuncSetAttribute(k_points<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t npts = (size_t)nz * nk;
+  unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
+  k_points<1><<<gr, T, smem, s>>>(A);
+  QCMG_CUDA(cudaGetLastError());
+  QCMG_CUDA(cudaMemcpyAsync(g, out.p, (size_t)2 * nz * nk * 8, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaStreamSynchronize(s));
+}
+
+// sum over the midpoint grid, per frequency: out[w] = mean_K M^-1
+__global__ void k_mean_inverse(const double2* __restrict__ inv, int nw, int nk, int LL,
+                               double2* __restrict__ out) {
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nw * LL;
+       idx += gridDim.x * blockDim.x) {
+    int w = idx / LL, e = idx % LL;
+    double sr = 0.0, si = 0.0;
+    for (int k = 0; k < nk; ++k) {
+      double2 v = inv[((size_t)w * nk + k) * LL + e];
+      sr += v.x;
+      si += v.y;
+    }
+    out[idx] = make_double2(sr / nk, si / nk);
+  }
+}
+
+void Lattice::projected(int nw, const double* w, int kside, int dimk, double* pgf, cudaStream_t s) {
+  std::vector<double> z(2 * nw);
+  for (int i = 0; i < nw; ++i) {
+    z[2 * i] = 0.0;
+    z[2 * i + 1] = w[i];
+  }
+  prepare(nw, z.data(), s);
+  PointArgs A = point_args(*this, nw);
+  int nk = 1;
+  A.gx = dimk >= 1 ? kside : 1;
+  A.gy = dimk >= 2 ? kside : 1;
+  A.gz = dimk >= 3 ? kside : 1;
+  nk = A.gx * A.gy * A.gz;
+  A.nk = nk;
+  A.off = dimk >= 1 ? 0.5 : 0.0;
+  const int LL = L * L;
+  DevBuf<double> inv, out;
+  inv.alloc((size_t)2 * nw * nk * LL);
+  out.alloc((size_t)2 * nw * LL);
+  A.out = (double2*)inv.p;
+  const int T = point_threads(L);
+  const size_t smem = (size_t)2 * L * L * T * 8;
+  QCMG_CUDA(cudaFuncSetAttribute(k_points<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const size_t npts = (size_t)nw * nk;
+  unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
+  k_points<2><<<gr, T, smem, s>>>(A);
+  k_mean_inverse<<<(nw * LL + 255) / 256, 256, 0, s>>>((const double2*)inv.p, nw, nk, LL,
+                                                       (double2*)out.p);
+  QCMG_CUDA(cudaGetLastError());
+  QCMG_CUDA(cudaMemcpyAsync(pgf, out.p, (size_t)2 * nw * LL * 8, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaStreamSynchronize(s));
+}
+
+}  // namespace qcmg
