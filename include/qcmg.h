@@ -187,6 +187,59 @@ int qcmg_apply_c(int L, int orb, int pm, int n_up, int n_dn, const double* x, do
 int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, const double* z,
                         double* G);
 
+/* ---------------------------------------------------------------------------
+ * Lattice integrals (CPT / VCA / CDMFT) over a cluster Green function.
+ *
+ * A lattice handle holds one spin block of a lattice model instance:
+ *   t(K) - t_c = Hdiff + sum_e v_e exp(2 pi i K.R[n_e]) |r_e><c_e|
+ * with K in the reduced (superlattice-dual) basis and R[n] the superlattice
+ * translations in the superlattice basis; Hdiff (L x L complex, row-major,
+ * interleaved re/im) is the k-independent difference between the lattice and
+ * cluster one-body matrices; gpos (L x 3) are the orbital positions in the
+ * superlattice basis (for periodization).  This is the data the reference's
+ * lattice_model_instance::set_V combines (src_qcm/CPT.cpp:22-64): R =
+ * lattice_model::neighbor, elements = lattice_operator::IGF_elem times the
+ * parameter values, Hdiff = H - Hc. */
+typedef struct qcmg_lattice qcmg_lattice;
+
+int qcmg_lattice_create(int L, int nR, const double* R, int nel, const int32_t* el_r,
+                        const int32_t* el_c, const int32_t* el_n, const double* el_v,
+                        const double* hdiff, const double* gpos, qcmg_lattice** out);
+int qcmg_lattice_destroy(qcmg_lattice* lat);
+
+/* Cluster Green function of the block: Q-matrix (e[M], v: L x M complex,
+ * column-major interleaved) and bath hybridization tcb (L x nb complex,
+ * column-major), eb[nb]: Gamma(z) = sum_i tcb_i tcb_i^+ / (z - eb_i).
+ * Replaces cluster_Green_function + hybridization_function
+ * (src_qcm/lattice_model_instance.cpp, src_ed/model_instance.hpp:1004-1017). */
+int qcmg_lattice_set_green(qcmg_lattice* lat, int M, const double* e, const double* v, int nb,
+                           const double* tcb, const double* eb);
+
+/* out = sum_w wt[w] (1/Nk) sum_K log|det(V(K, i w) G(i w) - 1)| on the grid
+ * K = (i/nkx, j/nky, l/nkz).  The caller combines spin blocks as the
+ * reference does (x2 for normal mixing).  Replaces the fixed-grid branch of
+ * lattice_model_instance::Potthoff_functional with SEF_integrand_k and
+ * QCM::k_integral_grid (src_qcm/lattice_model_instance.cpp:520-546,624-643,
+ * src_util/integrate.cpp:177-239). */
+int qcmg_sef_grid(qcmg_lattice* lat, int nw, const double* w, const double* wt, int nkx, int nky,
+                  int nkz, double* out);
+
+/* Periodized CPT Green function g(K, z) = (1/L) sum_ab Gcpt_ab(K,z)
+ * exp(2 pi i K.(x_b - x_a)) for nz complex frequencies z and nk reduced
+ * wavevectors K (nk x 3); g is nz x nk complex (interleaved).  Replaces
+ * set_Gcpt + lattice_model::periodize (src_qcm/CPT.cpp:76-86,171-176,
+ * src_qcm/lattice_model.cpp:724-740) for one band. */
+int qcmg_cpt_periodized(qcmg_lattice* lat, int nz, const double* z, int nk, const double* K,
+                        double* g);
+
+/* Projected (k-averaged) CPT Green function on the midpoint grid of side
+ * kside in dimk dimensions, at imaginary frequencies i w: pgf is nw blocks of
+ * L x L complex, row-major.  Replaces lattice_model_instance::
+ * projected_Green_function (src_qcm/CPT.cpp:283-345), the kernel of
+ * CDMFT_host. */
+int qcmg_cdmft_projected(qcmg_lattice* lat, int nw, const double* w, int kside, int dimk,
+                         double* pgf);
+
 #ifdef __cplusplus
 }
 #endif

@@ -59,6 +59,13 @@ SIGNATURES = {
                                   vp, c_int]),
     "qcmg_apply_c": (c_int, [c_int, c_int, c_int, c_int, c_int, vp, vp, c_double, c_uint]),
     "qcmg_green_function": (c_int, [c_int, c_int, vp, vp, c_int, vp, vp]),
+    "qcmg_lattice_create": (c_int, [c_int, c_int, vp, c_int, vp, vp, vp, vp, vp, vp,
+                                    ctypes.POINTER(vp)]),
+    "qcmg_lattice_destroy": (c_int, [vp]),
+    "qcmg_lattice_set_green": (c_int, [vp, c_int, vp, vp, c_int, vp, vp]),
+    "qcmg_sef_grid": (c_int, [vp, c_int, vp, vp, c_int, c_int, c_int, dbl_p]),
+    "qcmg_cpt_periodized": (c_int, [vp, c_int, vp, c_int, vp, vp]),
+    "qcmg_cdmft_projected": (c_int, [vp, c_int, vp, c_int, c_int, vp]),
 }
 
 

@@ -12,6 +12,7 @@
 #include "qcmg_internal.h"
 #include "qcmg_fxpath.h"
 #include "qcmg_krylov.h"
+#include "qcmg_lattice.h"
 
 namespace qcmg {
 
@@ -482,6 +483,123 @@ int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, 
     dG.alloc((size_t)2 * L * L * nz);
     green_function_batch(L, M, de.p, dv.p, nz, dz.p, dG.p, 0);
     QCMG_CUDA(cudaMemcpy(G, dG.p, (size_t)2 * L * L * nz * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
+int qcmg_lattice_create(int L, int nR, const double* R, int nel, const int32_t* el_r,
+                        const int32_t* el_c, const int32_t* el_n, const double* el_v,
+                        const double* hdiff, const double* gpos, qcmg_lattice** out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(out != nullptr, "out is NULL");
+    *out = nullptr;
+    QCMG_CHECK_ARG(L >= 1 && L <= 32, "L must be in 1..32");
+    QCMG_CHECK_ARG(nR >= 1 && R != nullptr, "at least one superlattice translation (R[0] = 0)");
+    QCMG_CHECK_ARG(nel >= 0 && (nel == 0 || (el_r && el_c && el_n && el_v)), "NULL element array");
+    QCMG_CHECK_ARG(hdiff && gpos, "NULL argument");
+    for (int k = 0; k < nel; ++k)
+      QCMG_CHECK_ARG(el_r[k] >= 0 && el_r[k] < L && el_c[k] >= 0 && el_c[k] < L && el_n[k] >= 0 &&
+                         el_n[k] < nR,
+                     "lattice element index out of range");
+    use_device();
+    auto* h = new qcmg_lattice();
+    try {
+      Lattice& t = h->lat;
+      t.device = g_device;
+      t.L = L;
+      t.nR = nR;
+      t.nel = nel;
+      QCMG_CUDA(cudaStreamCreateWithFlags(&t.stream, cudaStreamNonBlocking));
+      t.R.upload(R, (size_t)3 * nR, t.stream);
+      t.gpos.upload(gpos, (size_t)3 * L, t.stream);
+      t.hdiff.upload(hdiff, (size_t)2 * L * L, t.stream);
+      std::vector<int> r(el_r, el_r + nel), c(el_c, el_c + nel), n(el_n, el_n + nel);
+      if (nel) {
+        t.el_r.upload(r.data(), nel, t.stream);
+        t.el_c.upload(c.data(), nel, t.stream);
+        t.el_n.upload(n.data(), nel, t.stream);
+        t.el_v.upload(el_v, (size_t)2 * nel, t.stream);
+      }
+      QCMG_CUDA(cudaStreamSynchronize(t.stream));
+    } catch (...) {
+      if (h->lat.stream) cudaStreamDestroy(h->lat.stream);
+      delete h;
+      throw;
+    }
+    *out = h;
+  });
+}
+
+int qcmg_lattice_destroy(qcmg_lattice* h) {
+  return guarded([&] {
+    if (!h) return;
+    cudaSetDevice(h->lat.device);
+    if (h->lat.stream) {
+      cudaStreamSynchronize(h->lat.stream);
+      cudaStreamDestroy(h->lat.stream);
+    }
+    delete h;
+  });
+}
+
+int qcmg_lattice_set_green(qcmg_lattice* h, int M, const double* e, const double* v, int nb,
+                           const double* tcb, const double* eb) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h != nullptr, "NULL handle");
+    QCMG_CHECK_ARG(M >= 0 && nb >= 0, "negative size");
+    QCMG_CHECK_ARG((M == 0 || (e && v)) && (nb == 0 || (tcb && eb)), "NULL array");
+    std::lock_guard<std::mutex> lock(h->mu);
+    Lattice& t = h->lat;
+    QCMG_CUDA(cudaSetDevice(t.device));
+    t.M = M;
+    if (M) {
+      t.e.upload(e, M, t.stream);
+      t.v.upload(v, (size_t)2 * t.L * M, t.stream);
+    }
+    t.nb = nb;
+    if (nb) {
+      t.tcb.upload(tcb, (size_t)2 * t.L * nb, t.stream);
+      t.eb.upload(eb, nb, t.stream);
+    } else {
+      t.tcb.alloc(2);
+      t.eb.alloc(1);
+    }
+    QCMG_CUDA(cudaStreamSynchronize(t.stream));
+  });
+}
+
+int qcmg_sef_grid(qcmg_lattice* h, int nw, const double* w, const double* wt, int nkx, int nky,
+                  int nkz, double* out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h && w && wt && out, "NULL argument");
+    QCMG_CHECK_ARG(nw > 0 && nkx > 0 && nky > 0 && nkz > 0, "invalid grid");
+    std::lock_guard<std::mutex> lock(h->mu);
+    QCMG_CHECK_ARG(h->lat.M >= 0, "the Green function was not set");
+    QCMG_CUDA(cudaSetDevice(h->lat.device));
+    *out = h->lat.sef_grid(nw, w, wt, nkx, nky, nkz, h->lat.stream);
+  });
+}
+
+int qcmg_cpt_periodized(qcmg_lattice* h, int nz, const double* z, int nk, const double* K,
+                        double* g) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h && z && K && g, "NULL argument");
+    QCMG_CHECK_ARG(nz > 0 && nk > 0, "invalid sizes");
+    std::lock_guard<std::mutex> lock(h->mu);
+    QCMG_CHECK_ARG(h->lat.M >= 0, "the Green function was not set");
+    QCMG_CUDA(cudaSetDevice(h->lat.device));
+    h->lat.cpt(nz, z, nk, K, g, h->lat.stream);
+  });
+}
+
+int qcmg_cdmft_projected(qcmg_lattice* h, int nw, const double* w, int kside, int dimk,
+                         double* pgf) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h && w && pgf, "NULL argument");
+    QCMG_CHECK_ARG(nw > 0 && kside > 0 && dimk >= 0 && dimk <= 3, "invalid sizes");
+    std::lock_guard<std::mutex> lock(h->mu);
+    QCMG_CHECK_ARG(h->lat.M >= 0, "the Green function was not set");
+    QCMG_CUDA(cudaSetDevice(h->lat.device));
+    h->lat.projected(nw, w, kside, dimk, pgf, h->lat.stream);
   });
 }
 

@@ -124,7 +124,7 @@ __global__ void k_freq_prep(int L, int nw, const double2* __restrict__ G,  // nw
     }
     B[idx] = make_double2(gx, gy);
   }
-  if (threadIdx.x == 0) logdetG[w] = -ldet;  // log|det G| = -log|det G^-1|... (see below)
+  if (threadIdx.x == 0) logdetG[w] = ldet;  // the pivots are those of G itself
 }
 
 // ---------------------------------------------------------------------------

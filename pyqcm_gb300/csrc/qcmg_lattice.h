@@ -1,0 +1,42 @@
+// Lattice integrals over the cluster Green function (host declarations).
+#pragma once
+
+#include "qcmg_internal.h"
+
+namespace qcmg {
+
+// One spin block of a lattice model instance: inter-cluster hopping in
+// Fourier form, the k-independent difference Hdiff = H - Hc, the positions of
+// the Green-function orbitals, and the cluster Green function (Q-matrix and
+// bath hybridization) set separately.
+struct Lattice {
+  int device = 0;
+  int L = 0, nR = 0, nel = 0;
+  DevBuf<double> R;      // nR x 3, reduced superlattice coordinates
+  DevBuf<double> gpos;   // L x 3, reduced coordinates
+  DevBuf<double> hdiff;  // L x L complex, row-major
+  DevBuf<int> el_r, el_c, el_n;
+  DevBuf<double> el_v;   // nel complex
+  int M = -1;
+  DevBuf<double> e;      // M poles
+  DevBuf<double> v;      // L x M complex, column-major
+  int nb = 0;
+  DevBuf<double> tcb;    // L x nb complex, column-major
+  DevBuf<double> eb;     // nb
+  DevBuf<double> base, logdetG;
+  int prepared_nw = 0;
+  cudaStream_t stream = nullptr;
+
+  void prepare(int nw, const double* z, cudaStream_t s);
+  double sef_grid(int nw, const double* w, const double* wt, int nkx, int nky, int nkz,
+                  cudaStream_t s);
+  void cpt(int nz, const double* z, int nk, const double* K, double* g, cudaStream_t s);
+  void projected(int nw, const double* w, int kside, int dimk, double* pgf, cudaStream_t s);
+};
+
+}  // namespace qcmg
+
+struct qcmg_lattice {
+  qcmg::Lattice lat;
+  std::mutex mu;
+};
