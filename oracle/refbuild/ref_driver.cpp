@@ -20,6 +20,7 @@
 //   sigma LABEL SPIN RE IM TAG                -> ED::self_energy(z)
 //   omega LABEL TAG                           -> ED::Potthoff_functional (cluster part)
 // Lattice (QCM) commands, mirroring the pyqcm Python calls:
+//   ops MODEL                                 -> creates the cluster-only operators given by el
 //   lat_cluster MODEL x y z [x y z ...]       -> QCM::add_cluster + QCM::add_system
 //   lat_model NAME a1x a1y a1z [a2x a2y a2z]  -> QCM::new_lattice_model (unit cell = identity)
 //   lat_hop NAME lx ly lz AMP TAU SIGMA       -> QCM::hopping_operator
@@ -270,6 +271,9 @@ int main(int argc, char** argv) {
         size_t label; string tag; ss >> label >> tag;
         ED::Green_function_solve(label);
         put_scalar(tag, ED::Potthoff_functional(label));
+      } else if (cmd == "ops") {
+        string m; ss >> m;
+        create_ops(S, m);
       } else if (cmd == "lat_cluster") {
         string m; ss >> m;
         vector<vector3D<int64_t>> pos;

@@ -304,7 +304,10 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
         fx_matvec_f64(H, x, y, acc);
       else
         matvec(H, x, y, acc);
-      if (!(flags & QCMG_ASYNC)) QCMG_CUDA(cudaStreamSynchronize(H->stream));
+      if (!(flags & QCMG_ASYNC)) {
+        QCMG_CUDA(cudaStreamSynchronize(H->stream));
+        if (fx) fx_check_error(H);
+      }
       return;
     }
     H->xbuf.alloc(n);
@@ -317,6 +320,7 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
       matvec(H, H->xbuf.p, H->ybuf.p, acc);
     QCMG_CUDA(cudaMemcpyAsync(y, H->ybuf.p, n * 8, cudaMemcpyDeviceToHost, H->stream));
     QCMG_CUDA(cudaStreamSynchronize(H->stream));
+    if (fx) fx_check_error(H);
   });
 }
 
@@ -385,7 +389,7 @@ int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int6
     y.n = H->dim;
     fx_matvec(H, x, y, nullptr, 0.0);
     *Ey = y.E;
-    if (!(flags & QCMG_ASYNC)) QCMG_CUDA(cudaStreamSynchronize(H->stream));
+    if (!(flags & QCMG_ASYNC)) fx_check_error(H);
   });
 }
 

@@ -24,6 +24,8 @@ void fx_from_f64(const double* x, size_t n, FxVec& v, cudaStream_t s,
                  DevBuf<unsigned long long>& tmp);
 void fx_to_f64(const FxVec& v, double* x, cudaStream_t s);
 void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma);
+// Throws if a kernel of the fast path reported a bounded-wait failure.
+void fx_check_error(qcmg_hamiltonian* H);
 // y (+)= H x on FP64 device vectors through the fixed-point product.
 void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
 LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, int max_iter,

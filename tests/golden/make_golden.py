@@ -16,7 +16,8 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, HERE)
-from models import CASES, ZS, hubbard_cluster  # noqa: E402
+from models import CASES, LATTICE_CASES, ZS, hubbard_cluster  # noqa: E402
+sys.path.insert(0, os.path.join(ROOT))
 
 DRIVER = os.path.join(ROOT, "oracle", "_ref", "qcm_ref_driver")
 DT = {"f8": "<f8", "u4": "<u4", "c16": "<c16"}
@@ -84,6 +85,69 @@ def main():
             extra += [f"destroy clus {sec} 3 0 -1 dup", f"destroy clus {sec} 5 1 -1 ddn",
                       f"destroy clus {sec} 2 0 1 cup", f"destroy clus {sec} 6 1 1 cdn"]
         ed_case(tag, nx, ny, params, sec, n_bath=nb, af=af, extra=extra, gf=gf, gz=ZS)
+    for tag, c in LATTICE_CASES.items():
+        lattice_case(tag, c)
+
+def lattice_case(tag, c):
+    """Runs a lattice model through the reference's QCM layer."""
+    from pyqcm_gb300.lattice import legendre_frequency_grid
+    ns = len(c["sites"])
+    nb = c["n_bath"]
+    lines = ["gchar Hamiltonian_format F", "gint seed 0", f"model clus {ns} {nb}"]
+    if nb:
+        _, _, bops = hubbard_cluster(2, 2, nb)
+        for op, (typ, els) in bops.items():
+            if op.startswith("eb") or op.startswith("tb"):
+                for r, cc, v in els:
+                    lines.append(f"el clus {op} {typ} {r} {cc} {v!r}")
+        lines.append("ops clus")
+    lines.append("lat_cluster clus " + " ".join(f"{x} {y} {z}" for x, y, z in c["sites"]))
+    lines.append("lat_model L " + " ".join(" ".join(str(a) for a in v) for v in c["superlattice"]))
+    for op in c["ops"]:
+        if op[0] == "inter":
+            lines.append(f"lat_inter {op[1]} {op[2]!r} Hubbard")
+        elif op[0] == "hop":
+            lx, ly, lz = op[2]
+            lines.append(f"lat_hop {op[1]} {lx} {ly} {lz} {op[3]!r} {op[4]} {op[5]}")
+        elif op[0] == "dw":
+            qx, qy, qz = op[3]
+            lines.append(f"lat_dw {op[1]} {op[2]} {qx} {qy} {qz} {op[4]!r} {op[5]!r}")
+    for k, v in c["params"].items():
+        lines.append(f"lat_param {k} {v!r}")
+    lines.append(f"lat_sector {c['sector']}")
+    lines.append("lat_instance 0")
+    dim = len(c["superlattice"])
+    ks = [(0.0, 0.0, 0.0), (0.125, 0.0, 0.0), (0.25, 0.0, 0.0), (0.5, 0.0, 0.0)]
+    if dim == 2:
+        ks = [(0.0, 0.0, 0.0), (0.125, 0.25, 0.0), (0.25, 0.25, 0.0), (0.5, 0.0, 0.0)]
+    zs = [0.5 + 0.1j, -1.0 + 0.1j, 2.0 + 0.1j, 0.3j]
+    lines.append(f"lat_gper 0 gper {len(zs)} " + " ".join(f"{z.real!r} {z.imag!r}" for z in zs)
+                 + f" {len(ks)} " + " ".join(f"{a!r} {b!r} {d!r}" for a, b, d in ks))
+    lines.append("lat_dump 0 L")
+    lines.append(f"lat_tk 0 tk {len(ks)} " + " ".join(f"{a!r} {b!r} {d!r}" for a, b, d in ks))
+    w, wt = legendre_frequency_grid(1.0, 10.0, 4, 6, 4)
+    lines.append(f"lat_kgrid 8 {8 if dim >= 2 else 1} 1")
+    lines.append(f"lat_wgrid {len(w)} " + " ".join(repr(x) for x in w) + " "
+                 + " ".join(repr(x) for x in wt))
+    lines.append("lat_sef 0 sef")
+    lines.append("omega 0 omega_clus")
+    if nb:
+        beta = 50.0
+        wn = [(2 * n + 1) * np.pi / beta for n in range(20)]
+        lines.append("gint kgrid_side 8")
+        lines.append(f"lat_host 0 host {len(wn)} " + " ".join(repr(x) for x in wn) + " "
+                     + " ".join("1.0" for _ in wn))
+        lines.append("lat_varia eb1_1 eb2_1 tb1_1")
+        lines.append("lat_dist 0 dist0 3 -1.0 1.0 0.5")
+        lines.append("lat_dist 0 dist1 3 -1.2 0.8 0.45")
+    out = run_spec(lines)
+    out["sef_w"] = w
+    out["sef_wt"] = wt
+    out["gper_k"] = np.array(ks)
+    out["gper_z"] = np.array(zs)
+    np.savez_compressed(os.path.join(HERE, tag + ".npz"), **out)
+    print(tag, sorted(k for k in out if k != "spec"))
+
 
 if __name__ == "__main__":
     main()
