@@ -135,6 +135,15 @@ int qcmg_fx_to_f64(size_t n, const int64_t* q, int E, double* x, void* stream);
 int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int64_t* qy, int* Ey,
                    unsigned flags);
 
+/* out[k] = <V_k, w> for k < m: V is a device array of m device pointers to
+ * vectors of length n, w a device vector, out a host array of m doubles.
+ * Fixed-order (deterministic) two-level reduction on `stream`; allocates its
+ * device scratch for the call.  The projections of classical Gram-Schmidt
+ * reorthogonalization and of band Lanczos' inner products
+ * (src_ed/Hamiltonian/Lanczos.hpp:255-330 computes them one ddot at a time). */
+int qcmg_multidot(int m, const double* const* V, const double* w, size_t n, double* out,
+                  void* stream);
+
 /* Seeded start vector of the reference: std::default_random_engine(seed)
  * drawing std::normal_distribution(0,1), normalized.
  * Replaces random() (src_util/vector_num.cpp:114-119). */

@@ -355,6 +355,19 @@ int main(int argc, char** argv) {
           for (auto& g : T) { d = g.r; for (size_t i = 0; i < g.r; i++) for (size_t j = 0; j < g.c; j++) out.push_back(g(i, j)); }
           put(tag, "c16", {ks.size(), d, d}, out.data(), out.size());
         }
+      } else if (cmd == "lat_gc" || cmd == "lat_V" || cmd == "lat_gcpt") {
+        int label; string tag; double re, im; ss >> label >> tag >> re >> im;
+        cplx z(re, im);
+        matrix<cplx> M;
+        if (cmd == "lat_gc") {
+          M = QCM::cluster_Green_function(0, z, false, label, false);
+        } else {
+          double a, b, c; ss >> a >> b >> c;
+          vector3D<double> k(a, b, c);
+          if (cmd == "lat_V") M = QCM::V_matrix(z, k, false, label);
+          else M = QCM::CPT_Green_function(z, k, false, label);
+        }
+        put_cmat(tag, M);
       } else if (cmd == "lat_dump") {
         int label; string tag; ss >> label >> tag;
         auto& I = *lattice_model_instances.at(label);

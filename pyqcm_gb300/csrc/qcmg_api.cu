@@ -393,6 +393,23 @@ int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int6
   });
 }
 
+int qcmg_multidot(int m, const double* const* V, const double* w, size_t n, double* out,
+                  void* stream) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(m >= 0 && (m == 0 || (V && w && out)), "NULL argument");
+    QCMG_CHECK_ARG(m <= 4096, "at most 4096 vectors per call");
+    if (m == 0) return;
+    use_device();
+    cudaStream_t s = (cudaStream_t)stream;
+    DevBuf<double> part, res;
+    part.alloc((size_t)m * multidot_blocks(n));
+    res.alloc(m);
+    multidot_launch(m, V, w, n, part.p, res.p, s);
+    QCMG_CUDA(cudaMemcpyAsync(out, res.p, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+  });
+}
+
 int qcmg_seeded_vector(size_t dim, unsigned seed, double* out) {
   return guarded([&] {
     QCMG_CHECK_ARG(out != nullptr || dim == 0, "NULL output");

@@ -288,7 +288,7 @@ __device__ __forceinline__ void slab_range(uint32_t a, uint32_t du, uint32_t* e0
   *e1 = (du & 1u) ? (odd_start ? du : du - 1u) : du;
 }
 
-template <int INTER>
+template <int INTER, int MAXD>
 __global__ void __launch_bounds__(1024, 1) k_fx_passU2(FxProdArgs A) {
   extern __shared__ __align__(16) int64_t smem_slab[];
   __shared__ __align__(8) uint64_t bars[2];
@@ -341,12 +341,19 @@ __global__ void __launch_bounds__(1024, 1) k_fx_passU2(FxProdArgs A) {
     for (uint32_t i = tid; i < du; i += blockDim.x) {
       const uint32_t c = A.cnt_up[i];
       const uint32_t np = c & 0xffu, nt = c >> 8;
+      // all column indices of the row first (independent loads), then the
+      // gathers: one L2 round trip per row instead of one per hop
+      uint32_t ix[MAXD];
+#pragma unroll
+      for (int k = 0; k < MAXD; ++k) ix[k] = ((uint32_t)k < nt) ? A.ell_up[(size_t)k * du + i] : 0u;
       int64_t sp = 0, sn = 0;
-      uint32_t k = 0;
-#pragma unroll 4
-      for (; k < np; ++k) sp += view[A.ell_up[(size_t)k * du + i]];
-#pragma unroll 4
-      for (; k < nt; ++k) sn += view[A.ell_up[(size_t)k * du + i]];
+#pragma unroll
+      for (int k = 0; k < MAXD; ++k) {
+        if ((uint32_t)k < np)
+          sp += view[ix[k]];
+        else if ((uint32_t)k < nt)
+          sn += view[ix[k]];
+      }
       int64_t out = mul_fix(sp - sn, A.mt_up, A.sh_up);
       int64_t D = A.dup[i] + dda;
       if (INTER == QCMG_INTER_ONSITE) {
@@ -408,6 +415,56 @@ __global__ void __launch_bounds__(256) k_fx_passD2(FxProdArgs A) {
   }
 }
 
+// Pass D, third form: an item is one row band times a block of kColBlock
+// down states; the neighbour lists of the whole block are staged in shared
+// memory once (one pair of barriers per block instead of per state).
+constexpr int kColBlock = 16;
+constexpr int kMaxDegD = 64;
+
+__global__ void __launch_bounds__(256) k_fx_passD3(FxProdArgs A) {
+  __shared__ uint32_t s_off[kColBlock + 1], s_split[kColBlock];
+  __shared__ size_t s_cols[kColBlock * kMaxDegD];
+  const uint32_t du = A.du, dd = A.dd;
+  const uint32_t nblk = (dd + kColBlock - 1) / kColBlock;
+  const size_t items = (size_t)A.nbands * nblk;
+  for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
+    const uint32_t band = (uint32_t)(it / nblk), blk = (uint32_t)(it % nblk);
+    const uint32_t a0 = blk * kColBlock, a1 = min(dd, a0 + kColBlock);
+    const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
+    const uint32_t base_k = A.rp_dn[a0], total = A.rp_dn[a1] - base_k;
+    __syncthreads();
+    if (threadIdx.x <= a1 - a0) s_off[threadIdx.x] = A.rp_dn[a0 + threadIdx.x] - base_k;
+    if (threadIdx.x < a1 - a0) s_split[threadIdx.x] = A.rs_dn[a0 + threadIdx.x] - base_k;
+    for (uint32_t k = threadIdx.x; k < total; k += blockDim.x)
+      s_cols[k] = (size_t)A.col_dn[base_k + k] * du;
+    __syncthreads();
+    for (uint32_t c = 0; c < a1 - a0; ++c) {
+      const uint32_t k0 = s_off[c], ks = s_split[c], k1 = s_off[c + 1];
+      const size_t ybase = (size_t)(a0 + c) * du;
+      for (uint32_t i = r0 + threadIdx.x; i < r1; i += 2 * blockDim.x) {
+        const uint32_t i2 = i + blockDim.x;
+        const bool two = i2 < r1;
+        const uint32_t j2 = two ? i2 : i;
+        int64_t p0 = 0, n0 = 0, p1 = 0, n1 = 0;
+#pragma unroll 4
+        for (uint32_t k = k0; k < ks; ++k) {
+          const int64_t* col = A.x + s_cols[k];
+          p0 += __ldcg(col + i);
+          p1 += __ldcg(col + j2);
+        }
+#pragma unroll 4
+        for (uint32_t k = ks; k < k1; ++k) {
+          const int64_t* col = A.x + s_cols[k];
+          n0 += __ldcg(col + i);
+          n1 += __ldcg(col + j2);
+        }
+        A.y[ybase + i] += mul_fix(p0 - n0, A.mt_dn, A.sh_dn);
+        if (two) A.y[ybase + i2] += mul_fix(p1 - n1, A.mt_dn, A.sh_dn);
+      }
+    }
+  }
+}
+
 // ---------------------------------------------------------------------------
 // tables
 
@@ -459,7 +516,7 @@ static void build_unit_csr(const HalfOp& op, cudaStream_t s, DevBuf<uint32_t>& r
 static bool build_ell(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs,
                       const DevBuf<uint32_t>& col, uint32_t dim, int maxdeg, cudaStream_t s,
                       DevBuf<uint16_t>& ell, DevBuf<uint16_t>& cnt) {
-  if (dim > 65535u || maxdeg > 255 || dim == 0) return false;
+  if (dim > 65535u || maxdeg > 32 || dim == 0) return false;
   std::vector<uint32_t> hrp(dim + 1), hrs(dim);
   QCMG_CUDA(cudaMemcpyAsync(hrp.data(), rp.p, (dim + 1) * 4, cudaMemcpyDeviceToHost, s));
   QCMG_CUDA(cudaMemcpyAsync(hrs.data(), rs.p, dim * 4, cudaMemcpyDeviceToHost, s));
@@ -502,7 +559,7 @@ bool fx_prepare(qcmg_hamiltonian* H) {
   if (!ok) return false;
   build_unit_csr(H->dn, s, T.rp_dn, T.rs_dn, T.col_dn, &T.t_dn, &T.maxdeg_dn, &ok);
   if (!ok) return false;
-  if (T.maxdeg_dn > 64) return false;  // pass D stages at most 64 neighbour slabs
+  if (T.maxdeg_dn > kMaxDegD) return false;  // pass D stages at most 64 neighbours per state
   // pass U with bulk-copied slabs: ELL tables and the number of buffers
   T.nbuf = 0;
   {
@@ -684,11 +741,26 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
       QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
       kern<<<g2, 1024, smem2, s>>>(A);
     };
-    switch (H->inter_kind) {
-      case QCMG_INTER_NONE: launchU2(k_fx_passU2<QCMG_INTER_NONE>); break;
-      case QCMG_INTER_ONSITE: launchU2(k_fx_passU2<QCMG_INTER_ONSITE>); break;
-      default: launchU2(k_fx_passU2<QCMG_INTER_GENERAL>); break;
-    }
+    auto byinter = [&](auto k0, auto k1, auto k2) {
+      switch (H->inter_kind) {
+        case QCMG_INTER_NONE: launchU2(k0); break;
+        case QCMG_INTER_ONSITE: launchU2(k1); break;
+        default: launchU2(k2); break;
+      }
+    };
+    const int md = T.maxdeg_up;
+    if (md <= 8)
+      byinter(k_fx_passU2<QCMG_INTER_NONE, 8>, k_fx_passU2<QCMG_INTER_ONSITE, 8>,
+              k_fx_passU2<QCMG_INTER_GENERAL, 8>);
+    else if (md <= 16)
+      byinter(k_fx_passU2<QCMG_INTER_NONE, 16>, k_fx_passU2<QCMG_INTER_ONSITE, 16>,
+              k_fx_passU2<QCMG_INTER_GENERAL, 16>);
+    else if (md <= 24)
+      byinter(k_fx_passU2<QCMG_INTER_NONE, 24>, k_fx_passU2<QCMG_INTER_ONSITE, 24>,
+              k_fx_passU2<QCMG_INTER_GENERAL, 24>);
+    else
+      byinter(k_fx_passU2<QCMG_INTER_NONE, 32>, k_fx_passU2<QCMG_INTER_ONSITE, 32>,
+              k_fx_passU2<QCMG_INTER_GENERAL, 32>);
   } else {
     switch (H->inter_kind) {
       case QCMG_INTER_NONE: launchU(k_fx_passU<QCMG_INTER_NONE>); break;
@@ -698,9 +770,9 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
   }
   QCMG_CUDA(cudaGetLastError());
   // pass D
-  const size_t items = (size_t)A.nbands * H->dd;
+  const size_t items = (size_t)A.nbands * ((H->dd + kColBlock - 1) / kColBlock);
   const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>(items, (size_t)sms * 8));
-  k_fx_passD2<<<gD, 256, 0, s>>>(A);
+  k_fx_passD3<<<gD, 256, 0, s>>>(A);
   QCMG_CUDA(cudaGetLastError());
   y.E = Eo;
   y.mb = kFxBits;

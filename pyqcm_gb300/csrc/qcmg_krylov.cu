@@ -73,6 +73,22 @@ __global__ void __launch_bounds__(256) k_multiaxpy(const double* const* __restri
   }
 }
 
+// Block count of a multi-dot over n elements (fixed: deterministic order).
+int multidot_blocks(size_t n) {
+  return (int)std::max<size_t>(1, std::min<size_t>((n + kTile - 1) / kTile, 2 * 152));
+}
+
+// Launches the two kernels of a multi-dot: part (m x nblocks doubles) is
+// scratch, every element of it read by the second kernel is first written
+// by the first; out (m doubles, device) receives the result.
+void multidot_launch(int m, const double* const* V, const double* w, size_t n, double* part,
+                     double* out, cudaStream_t s) {
+  const int nb = multidot_blocks(n);
+  k_multidot<<<nb, 256, m * sizeof(double), s>>>(V, m, w, n, part);
+  k_multidot_final<<<(m + 127) / 128, 128, 0, s>>>(part, nb, m, out);
+  QCMG_CUDA(cudaGetLastError());
+}
+
 struct MultiOps {
   DevBuf<const double*> ptrs;
   DevBuf<double> part, coef;

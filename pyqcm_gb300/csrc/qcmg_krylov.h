@@ -19,6 +19,10 @@ struct BandResult {
   std::vector<double> Q;      // p x M, row-major
 };
 
+int multidot_blocks(size_t n);
+void multidot_launch(int m, const double* const* V, const double* w, size_t n, double* part,
+                     double* out, cudaStream_t s);
+
 void seeded_vector(size_t dim, unsigned seed, double* out);
 
 LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,

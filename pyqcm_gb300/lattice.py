@@ -86,6 +86,12 @@ class LatticeModel:
         self.ops = {}
         self.target_sectors = None
         self.params = {}
+        # the chemical potential is always present, -1 per site and spin
+        # (lattice_model::add_chemical_potential, src_qcm/lattice_model.cpp:286-295)
+        mu = self._op("mu", "one-body")
+        no = cluster.n_orb
+        for i in range(len(self.sites)):
+            mu.intra += [(i, i, -1.0), (i + no, i + no, -1.0)]
 
     # -- geometry
     def _fold(self, r):

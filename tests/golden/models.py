@@ -77,25 +77,25 @@ CASES = {
 
 # Lattice golden cases.  Each: cluster sites, superlattice, lattice operators
 # [(kind, name, args)], cluster-only operators from hubbard_cluster (bath),
-# parameters (lattice names; cluster values 'name_1'), sector.
+# parameters (lattice names; cluster values 'name_1'), sector.  The chemical
+# potential 'mu' is the lattice model's built-in operator (-1 per site and
+# spin), as in the reference (src_qcm/lattice_model.cpp:286-295).
 LATTICE_CASES = {
     "lat_chain8": dict(
         sites=[(i, 0, 0) for i in range(8)], superlattice=[(8, 0, 0)], n_bath=0,
-        ops=[("inter", "U", 1.0), ("hop", "t", (1, 0, 0), -1.0, 1, 0),
-             ("hop", "mu", (0, 0, 0), -1.0, 0, 0)],
+        ops=[("inter", "U", 1.0), ("hop", "t", (1, 0, 0), -1.0, 1, 0)],
         params={"t": 1.0, "U": 4.0, "mu": 2.0}, sector="R0:N8:S0"),
     "lat_vca2x2_af": dict(
         sites=[(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)], superlattice=[(2, 0, 0), (0, 2, 0)],
         n_bath=0,
         ops=[("inter", "U", 1.0), ("hop", "t", (1, 0, 0), -1.0, 1, 0),
-             ("hop", "t", (0, 1, 0), -1.0, 1, 0), ("hop", "mu", (0, 0, 0), -1.0, 0, 0),
-             ("dw", "M", "Z", (1, 1, 0), 1.0, 0.0)],
+             ("hop", "t", (0, 1, 0), -1.0, 1, 0), ("dw", "M", "Z", (1, 1, 0), 1.0, 0.0)],
         params={"t": 1.0, "U": 8.0, "mu": 4.0, "M": 0.0, "M_1": 0.15}, sector="R0:N4:S0"),
     "lat_cdmft2x2_b4": dict(
         sites=[(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)], superlattice=[(2, 0, 0), (0, 2, 0)],
         n_bath=4,
         ops=[("inter", "U", 1.0), ("hop", "t", (1, 0, 0), -1.0, 1, 0),
-             ("hop", "t", (0, 1, 0), -1.0, 1, 0), ("hop", "mu", (0, 0, 0), -1.0, 0, 0)],
+             ("hop", "t", (0, 1, 0), -1.0, 1, 0)],
         params={"t": 1.0, "U": 4.0, "mu": 2.0, "eb1_1": -1.0, "eb2_1": 1.0, "eb3_1": -0.6,
                 "eb4_1": 0.6, "tb1_1": 0.5, "tb2_1": 0.5, "tb3_1": 0.4, "tb4_1": 0.4},
         sector="R0:N8:S0"),

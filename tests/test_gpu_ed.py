@@ -249,3 +249,20 @@ def test_fixed_point_product_4x4_full_sector(pg):
     assert err <= 1e-13 * float(y64.abs().max())
     del qx, qy, y_fx, y64, x
     torch.cuda.empty_cache()
+
+
+def test_multidot_against_numpy(pg):
+    torch = _torch()
+    from pyqcm_gb300 import _lib
+    gen = torch.Generator(device="cuda").manual_seed(11)
+    n, m = 1_000_003, 7
+    V = [torch.randn(n, dtype=torch.float64, device="cuda", generator=gen) for _ in range(m)]
+    w = torch.randn(n, dtype=torch.float64, device="cuda", generator=gen)
+    ptrs = torch.tensor([v.data_ptr() for v in V], dtype=torch.int64, device="cuda")
+    out = np.zeros(m)
+    _lib.check(pg.lib().qcmg_multidot(m, ptrs.data_ptr(), w.data_ptr(), n, _lib.ptr(out), None))
+    ref = np.array([float(torch.dot(v, w)) for v in V])
+    assert np.max(np.abs(out - ref)) < 1e-12 * np.sqrt(n)
+    out2 = np.zeros(m)
+    _lib.check(pg.lib().qcmg_multidot(m, ptrs.data_ptr(), w.data_ptr(), n, _lib.ptr(out2), None))
+    assert np.array_equal(out, out2)  # deterministic
