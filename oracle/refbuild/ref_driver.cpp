@@ -418,6 +418,9 @@ int main(int argc, char** argv) {
       } else {
         throw runtime_error("unknown spec command: " + cmd);
       }
+      // A token the stream could not read leaves zeros behind: refuse it
+      // (reading to the end of the line, as the list commands do, is fine).
+      if (ss.fail() && !ss.eof()) throw runtime_error("malformed arguments in spec line: " + line.substr(0, 80));
     }
   } catch (std::exception& e) {
     cerr << "oracle driver error: " << e.what() << endl;

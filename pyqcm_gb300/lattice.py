@@ -361,9 +361,12 @@ class LatticeInstance:
 
     def CDMFT_distance(self, bath_values):
         """sum_w w_n |Gamma(i w; p) + G_host(i w)|^2 dw / dim^2, x2 for normal
-        mixing (src_qcm/CPT.cpp:519-555).  bath_values: {cluster param: value}."""
+        mixing (src_qcm/CPT.cpp:519-555).  bath_values: {param: value}, named
+        as the lattice model names cluster parameters ('eb1_1' is eb1 of
+        cluster 1), the bare cluster name also accepted."""
         vals = dict(self.cluster.values)
-        vals.update(bath_values)
+        for name, x in bath_values.items():
+            vals[name[:-2] if name.endswith("_1") else name] = float(x)
         inst = ModelInstance(self.model.cluster, vals, self.model.target_sectors)
         inst.mixing = self.cluster.mixing
         w = self._host_freqs

@@ -39,6 +39,12 @@ def run_spec(lines):
         return out
 
 
+def num(x):
+    """A number as the driver's stream parser reads it (numpy 2 scalars repr
+    as 'np.float64(...)', which would silently parse as 0)."""
+    return repr(float(x))
+
+
 def model_lines(name, ns, nb, ops):
     lines = [f"model {name} {ns} {nb}"]
     for op, (typ, els) in ops.items():
@@ -127,15 +133,15 @@ def lattice_case(tag, c):
     lines.append(f"lat_tk 0 tk {len(ks)} " + " ".join(f"{a!r} {b!r} {d!r}" for a, b, d in ks))
     w, wt = legendre_frequency_grid(1.0, 10.0, 4, 6, 4)
     lines.append(f"lat_kgrid 8 {8 if dim >= 2 else 1} 1")
-    lines.append(f"lat_wgrid {len(w)} " + " ".join(repr(x) for x in w) + " "
-                 + " ".join(repr(x) for x in wt))
+    lines.append(f"lat_wgrid {len(w)} " + " ".join(num(x) for x in w) + " "
+                 + " ".join(num(x) for x in wt))
     lines.append("lat_sef 0 sef")
     lines.append("omega 0 omega_clus")
     if nb:
         beta = 50.0
         wn = [(2 * n + 1) * np.pi / beta for n in range(20)]
         lines.append("gint kgrid_side 8")
-        lines.append(f"lat_host 0 host {len(wn)} " + " ".join(repr(x) for x in wn) + " "
+        lines.append(f"lat_host 0 host {len(wn)} " + " ".join(num(x) for x in wn) + " "
                      + " ".join("1.0" for _ in wn))
         lines.append("lat_varia eb1_1 eb2_1 tb1_1")
         lines.append("lat_dist 0 dist0 3 -1.0 1.0 0.5")
