@@ -1,12 +1,13 @@
 """Benchmark: Lanczos H.psi throughput on the 4x4 Hubbard cluster at half
 filling (16 sites, N=16, Sz=0, sector dimension 165,636,900, FP64 vectors).
 
-A step is one Hamiltonian-vector product y = H x of that sector, the product
-every Lanczos / band-Lanczos iteration performs.  value = algorithmic bytes
-(24 B per basis state: read x, read y, write y) x steps / device time,
-with both vectors (1.33 GB each, larger than L2) resident in HBM.
-e2e = the same metric through the public host API (x copied in from pinned
-host memory, y copied back, every step).
+A step is one Hamiltonian-vector product y <- y + H x of that sector (the
+reference's mult_add, performed by every Lanczos / band-Lanczos iteration).
+value = algorithmic bytes (24 B per basis state: read x, read y, write y)
+x steps / device time, with both vectors (1.33 GB each, larger than L2)
+resident in HBM.  e2e = the same metric through the public host API
+(Hamiltonian.mult_add: x and y copied in from pinned host memory, y copied
+back, every step).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl qcmg|reference]
 
@@ -30,19 +31,21 @@ sys.path.insert(0, os.path.join(ROOT, "tests", "golden"))
 METRIC = "lanczos_hpsi_gbs"
 UNIT = "GB/s"
 NX, NY = 4, 4
+NEL = None  # electrons (None: half filling)
 PARAMS = {"t": 1.0, "U": 8.0, "mu": 4.0}
 BYTES_PER_STATE = 24
 
 
 def sector_of(nx, ny):
-    n = nx * ny
+    """(sector, n_up, n_dn): half filling, or NEL electrons when set."""
+    n = NEL if NEL else nx * ny
     return f"R0:N{n}:S{n % 2}", (n + n % 2) // 2, n // 2
 
 
 def workload_config(dim=165636900):
     sec = sector_of(NX, NY)[0]
     return {"workload": f"{NX}x{NY} Hubbard cluster, t=1 U=8 mu=4, sector {sec} "
-                        f"(dim {dim:,}), y = H x",
+                        f"(dim {dim:,}), y <- y + H x",
             "dim": dim, "bytes_per_step": BYTES_PER_STATE * dim,
             "l2": "inputs larger than L2", "parallelism": "replicas"}
 
@@ -198,13 +201,17 @@ def run_gpu(args):
         E, mb = pg._lib.c_int(), pg._lib.c_int()
         pg._lib.check(pg.lib().qcmg_fx_from_f64(D, x.data_ptr(), qx.data_ptr(), E, mb,
                                                 stream.cuda_stream))
-        step = lambda: H.matvec_fx_device(qx.data_ptr(), E.value, mb.value, qy.data_ptr(),
-                                          asynchronous=True)
+        qy.copy_(qx)
+        ey = [E.value]
+
+        def step():  # y <- y + H x
+            ey[0] = H.matvec_fx_device(qx.data_ptr(), E.value, mb.value, qy.data_ptr(),
+                                       asynchronous=True, Ey_in=ey[0])
         y = qy
-        kernels = ["k_fx_passU", "k_fx_passD"]
+        kernels = ["k_fx_passU4", "k_fx_passD4"]
     else:
-        y = torch.zeros(D, dtype=torch.float64, device="cuda")
-        step = lambda: H.matvec_device(x.data_ptr(), y.data_ptr(), asynchronous=True)
+        y = x.clone()
+        step = lambda: H.matvec_device(x.data_ptr(), y.data_ptr(), asynchronous=True, accumulate=True)
         kernels = ["k_matvec_f64"]
     for _ in range(args.warmup):
         step()
@@ -241,20 +248,22 @@ def run_gpu(args):
     achieved = bytes_step / (avg_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
 
-    # e2e through the public host API: pinned host x in, y out, every step.
+    # e2e through the public host API (Hamiltonian.mult_add, the reference's
+    # mult_add): pinned host x and y in, y out, every step.
     xh = torch.empty(D, dtype=torch.float64, pin_memory=True)
     xh.copy_(x.cpu())
     xn = xh.numpy()
-    ev0 = torch.cuda.Event(enable_timing=True)
+    yh = torch.zeros(D, dtype=torch.float64, pin_memory=True)
+    yn = yh.numpy()
     e2e_steps = max(2, min(args.steps, 5))
     H.set_stream(0)
-    H.matvec(xn)  # warm-up of the staging buffers
+    H.mult_add(xn, yn)  # warm-up of the staging buffers
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        yh = H.matvec(xn)
+        H.mult_add(xn, yn)
     e2e_s = (time.perf_counter() - t0) / e2e_steps
     e2e_val = bytes_step * world / e2e_s / 1e9
-    del ev0, yh
+    del yh, yn
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": total_ms / args.steps,
@@ -264,7 +273,7 @@ def run_gpu(args):
                          "frac": achieved / peak, "traffic": profile_traffic(),
                          "peak_kind": peak_kind, "kernels": kernels},
             "clocks": clocks.summary(),
-            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 8 * D,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 16 * D,
                     "d2h_bytes_per_step": 8 * D},
             "gpu_launches": args.steps * len(kernels)}
     if rank == 0 and not args.no_cpu_baseline:
@@ -288,9 +297,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cluster", default="4x4",
                     help="NXxNY Hubbard cluster at half filling (profiling of smaller cases)")
+    ap.add_argument("--electrons", type=int, default=None,
+                    help="electrons in the sector (default: half filling)")
     args = ap.parse_args()
-    global NX, NY
+    global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))
+    NEL = args.electrons
     if args.impl == "reference":
         run_reference(args)
     else:

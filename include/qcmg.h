@@ -128,10 +128,12 @@ int qcmg_fx_from_f64(size_t n, const double* x, int64_t* q, int* E, int* mb, voi
 int qcmg_fx_to_f64(size_t n, const int64_t* q, int E, double* x, void* stream);
 
 /* y = H x on fixed-point device vectors (length dim): x given by (qx, Ex,
- * mbx); the result's exponent is returned in *Ey (|qy| < 2^56).  Launches on
- * the handle's stream; QCMG_ASYNC returns without waiting.  Same product as
- * qcmg_matvec (Hamiltonian_Factorized::mult_add), exact integer arithmetic
- * on the hops and one rounding per diagonal term. */
+ * mbx); the result's exponent is returned in *Ey (|qy| < 2^56).  With
+ * QCMG_ACCUMULATE, y = y + H x: *Ey gives the input y's exponent on entry
+ * (|qy| < 2^56) and the result's on return.  Launches on the handle's
+ * stream; QCMG_ASYNC returns without waiting.  Same product as qcmg_matvec
+ * (Hamiltonian_Factorized::mult_add), exact integer arithmetic on the hops
+ * and one rounding per diagonal term. */
 int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int64_t* qy, int* Ey,
                    unsigned flags);
 

@@ -38,7 +38,8 @@ def _sources():
 
 def _stamp(srcs):
     h = hashlib.sha256()
-    for s in srcs + sorted(glob.glob(os.path.join(CSRC, "*.h"))) + [os.path.join(ROOT, "include", "qcmg.h")]:
+    hdrs = sorted(glob.glob(os.path.join(CSRC, "*.h")) + glob.glob(os.path.join(CSRC, "*.cuh")))
+    for s in srcs + hdrs + [os.path.join(ROOT, "include", "qcmg.h")]:
         with open(s, "rb") as f:
             h.update(f.read())
     h.update(" ".join(_flags()).encode())

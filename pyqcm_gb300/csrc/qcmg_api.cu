@@ -10,6 +10,7 @@
 
 #include "qcmg.h"
 #include "qcmg_internal.h"
+#include "qcmg_fx.cuh"
 #include "qcmg_fxpath.h"
 #include "qcmg_krylov.h"
 #include "qcmg_lattice.h"
@@ -387,7 +388,18 @@ int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int6
     x.c = 1.0;
     y.buf.borrow(qy, H->dim);
     y.n = H->dim;
-    fx_matvec(H, x, y, nullptr, 0.0);
+    if (flags & QCMG_ACCUMULATE) {
+      // the input y, in place: pass U reads and writes each entry once
+      FxVec yin;
+      yin.buf.borrow(qy, H->dim);
+      yin.n = H->dim;
+      yin.E = *Ey;
+      yin.mb = kFxBits;
+      yin.c = 1.0;
+      fx_matvec(H, x, y, &yin, 1.0);
+    } else {
+      fx_matvec(H, x, y, nullptr, 0.0);
+    }
     *Ey = y.E;
     if (!(flags & QCMG_ASYNC)) fx_check_error(H);
   });

@@ -16,12 +16,14 @@
 #include <algorithm>
 #include <cfloat>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
 #include "qcmg_fx.cuh"
 #include "qcmg_tma.cuh"
 #include "qcmg_fxpath.h"
+#include "qcmg_fxprod.h"
 #include "qcmg_internal.h"
 #include "qcmg_tridiag.h"
 
@@ -187,284 +189,6 @@ __global__ void k_fx_axpy(int64_t* __restrict__ g, const int64_t* __restrict__ q
 }
 
 // ---------------------------------------------------------------------------
-// product kernels
-
-struct FxProdArgs {
-  uint32_t du, dd;
-  int L;
-  // up half-operator: row i has positive hops cols[rp[i]..rs[i]) and negative
-  // hops cols[rs[i]..rp[i+1])
-  const uint32_t* rp_up;
-  const uint32_t* rs_up;
-  const uint32_t* col_up;
-  const uint32_t* rp_dn;
-  const uint32_t* rs_dn;
-  const uint32_t* col_dn;
-  const int64_t* dup;  // fixed-point diagonal of each half basis (scale 2^-G)
-  const int64_t* ddn;
-  const uint32_t* bin_up;
-  const uint32_t* bin_dn;
-  int64_t U;        // on-site interaction (scale 2^-G)
-  const int64_t* wdn;  // dd x L cross table (scale 2^-G), general interactions
-  int64_t mt_up, mt_dn;  // hop magnitudes (mantissas)
-  int sh_up, sh_dn;      // shifts of the hop terms
-  int sh_d;              // shift of the diagonal term
-  const int64_t* yin;    // accumulated input (may alias y) or null
-  int64_t m_in;
-  int sh_in;
-  const int64_t* x;
-  int64_t* y;
-  uint32_t band;   // rows per band (pass D)
-  uint32_t nbands;
-  // ELL form of the up half-operator: column k of row i at ell[k*du + i]
-  // (positive hops first); cnt[i] = (number of positive) | (total << 8)
-  const uint16_t* ell_up;
-  const uint16_t* cnt_up;
-  int nbuf;      // shared-memory slab buffers of pass U (1 or 2)
-  int* err;      // set to 1 when a bounded wait gives up
-};
-
-template <int INTER>
-__global__ void __launch_bounds__(512) k_fx_passU(FxProdArgs A) {
-  extern __shared__ int64_t xs[];
-  const uint32_t du = A.du;
-  for (uint32_t a = blockIdx.x; a < A.dd; a += gridDim.x) {
-    const size_t base = (size_t)a * du;
-    __syncthreads();
-    for (uint32_t i = threadIdx.x; i < du; i += blockDim.x) xs[i] = A.x[base + i];
-    __syncthreads();
-    const int64_t dda = A.ddn[a];
-    const uint32_t dbits = A.bin_dn[a];
-    for (uint32_t i = threadIdx.x; i < du; i += blockDim.x) {
-      const uint32_t k0 = A.rp_up[i], ks = A.rs_up[i], k1 = A.rp_up[i + 1];
-      int64_t sp = 0, sn = 0;
-      for (uint32_t k = k0; k < ks; ++k) sp += xs[A.col_up[k]];
-      for (uint32_t k = ks; k < k1; ++k) sn += xs[A.col_up[k]];
-      int64_t out = mul_fix(sp - sn, A.mt_up, A.sh_up);
-      int64_t D = A.dup[i] + dda;
-      if (INTER == QCMG_INTER_ONSITE) {
-        D += A.U * (int64_t)__popc(A.bin_up[i] & dbits);
-      } else if (INTER == QCMG_INTER_GENERAL) {
-        uint32_t u = A.bin_up[i];
-        const int64_t* w = A.wdn + (size_t)a * A.L;
-        while (u) {
-          D += w[__ffs(u) - 1];
-          u &= u - 1;
-        }
-      }
-      out += mul_fix(xs[i], D, A.sh_d);
-      if (A.yin) out += mul_fix(A.yin[base + i], A.m_in, A.sh_in);
-      A.y[base + i] = out;
-    }
-  }
-}
-
-__global__ void __launch_bounds__(256) k_fx_passD(FxProdArgs A) {
-  const uint32_t du = A.du, dd = A.dd;
-  const size_t items = (size_t)A.nbands * dd;
-  for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
-    const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
-    const uint32_t k0 = A.rp_dn[a], ks = A.rs_dn[a], k1 = A.rp_dn[a + 1];
-    for (uint32_t i = r0 + threadIdx.x; i < r1; i += blockDim.x) {
-      int64_t sp = 0, sn = 0;
-      for (uint32_t k = k0; k < ks; ++k) sp += __ldcg(A.x + (size_t)A.col_dn[k] * du + i);
-      for (uint32_t k = ks; k < k1; ++k) sn += __ldcg(A.x + (size_t)A.col_dn[k] * du + i);
-      const size_t idx = (size_t)a * du + i;
-      A.y[idx] += mul_fix(sp - sn, A.mt_dn, A.sh_dn);
-    }
-  }
-}
-
-// Pass U with the slab staged by bulk (TMA) copies, double-buffered: one
-// persistent 1024-thread CTA per SM computes slab a from one buffer while
-// the copy engine fills the other with slab a + gridDim.  A slab starts at
-// byte a*du*8; when du is odd that is 8 mod 16 for odd a, so each copy moves
-// the 16-byte-aligned interior and thread 0 loads the (at most one) element
-// left over at either end.
-__device__ __forceinline__ void slab_range(uint32_t a, uint32_t du, uint32_t* e0, uint32_t* e1) {
-  const bool odd_start = (du & 1u) && (a & 1u);
-  *e0 = odd_start ? 1u : 0u;
-  *e1 = (du & 1u) ? (odd_start ? du : du - 1u) : du;
-}
-
-template <int INTER, int MAXD>
-__global__ void __launch_bounds__(1024, 1) k_fx_passU2(FxProdArgs A) {
-  extern __shared__ __align__(16) int64_t smem_slab[];
-  __shared__ __align__(8) uint64_t bars[2];
-  const uint32_t du = A.du, dd = A.dd;
-  const uint32_t stride = ((du + 2u) + 1u) & ~1u;  // elements per buffer (16-byte multiple)
-  const int tid = threadIdx.x;
-  if (tid == 0) {
-    mbar_init(&bars[0], 1);
-    mbar_init(&bars[1], 1);
-    fence_barrier_init();
-  }
-  __syncthreads();
-  auto issue = [&](uint32_t a, int b) {
-    uint32_t e0, e1;
-    slab_range(a, du, &e0, &e1);
-    int64_t* dst = smem_slab + (size_t)b * stride + 2 * e0;  // view = buf + e0 (see below)
-    const int64_t* src = A.x + (size_t)a * du + e0;
-    const unsigned bytes = (e1 - e0) * 8u;
-    mbar_arrive_expect_tx(&bars[b], bytes);
-    bulk_g2s(dst, src, bytes, &bars[b]);
-  };
-  const uint32_t G = gridDim.x;
-  if (tid == 0) {
-    if (blockIdx.x < dd) issue(blockIdx.x, 0);
-    if (A.nbuf == 2 && blockIdx.x + G < dd) issue(blockIdx.x + G, 1);
-  }
-  unsigned parity[2] = {0u, 0u};
-  int j = 0;
-  for (uint32_t a = blockIdx.x; a < dd; a += G, ++j) {
-    const int b = (A.nbuf == 2) ? (j & 1) : 0;
-    const bool ok = mbar_wait_bounded(&bars[b], parity[b]);
-    if (__syncthreads_or(!ok)) {  // CTA-uniform decision: every thread leaves together
-      if (tid == 0) atomicExch(A.err, 1);
-      return;
-    }
-    parity[b] ^= 1u;
-    uint32_t e0, e1;
-    slab_range(a, du, &e0, &e1);
-    // view[i] = slab element i; the copy landed at buf + 2*e0 elements, so
-    // view = buf + e0 (view[e0] = buf[2 e0]).
-    int64_t* view = smem_slab + (size_t)b * stride + e0;
-    const size_t base = (size_t)a * du;
-    if (tid == 0) {
-      if (e0 == 1u) view[0] = A.x[base];
-      if (e1 == du - 1u) view[du - 1] = A.x[base + du - 1];
-    }
-    __syncthreads();
-    const int64_t dda = A.ddn[a];
-    const uint32_t dbits = A.bin_dn[a];
-    for (uint32_t i = tid; i < du; i += blockDim.x) {
-      const uint32_t c = A.cnt_up[i];
-      const uint32_t np = c & 0xffu, nt = c >> 8;
-      // all column indices of the row first (independent loads), then the
-      // gathers: one L2 round trip per row instead of one per hop
-      uint32_t ix[MAXD];
-#pragma unroll
-      for (int k = 0; k < MAXD; ++k) ix[k] = ((uint32_t)k < nt) ? A.ell_up[(size_t)k * du + i] : 0u;
-      int64_t sp = 0, sn = 0;
-#pragma unroll
-      for (int k = 0; k < MAXD; ++k) {
-        if ((uint32_t)k < np)
-          sp += view[ix[k]];
-        else if ((uint32_t)k < nt)
-          sn += view[ix[k]];
-      }
-      int64_t out = mul_fix(sp - sn, A.mt_up, A.sh_up);
-      int64_t D = A.dup[i] + dda;
-      if (INTER == QCMG_INTER_ONSITE) {
-        D += A.U * (int64_t)__popc(A.bin_up[i] & dbits);
-      } else if (INTER == QCMG_INTER_GENERAL) {
-        uint32_t u = A.bin_up[i];
-        const int64_t* w = A.wdn + (size_t)a * A.L;
-        while (u) {
-          D += w[__ffs(u) - 1];
-          u &= u - 1;
-        }
-      }
-      out += mul_fix(view[i], D, A.sh_d);
-      if (A.yin) out += mul_fix(A.yin[base + i], A.m_in, A.sh_in);
-      A.y[base + i] = out;
-    }
-    __syncthreads();  // buffer b is free again
-    const uint32_t next = a + (A.nbuf == 2 ? 2u : 1u) * G;
-    if (tid == 0 && next < dd) {
-      fence_proxy_async_smem();
-      issue(next, b);
-    }
-  }
-}
-
-// Pass D, second form: the neighbour slab offsets of the item are staged in
-// shared memory and each thread sums two rows at once (independent loads).
-__global__ void __launch_bounds__(256) k_fx_passD2(FxProdArgs A) {
-  __shared__ size_t offs[64];
-  const uint32_t du = A.du, dd = A.dd;
-  const size_t items = (size_t)A.nbands * dd;
-  for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
-    const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
-    const uint32_t k0 = A.rp_dn[a], ks = A.rs_dn[a], k1 = A.rp_dn[a + 1];
-    const int np = (int)(ks - k0), nt = (int)(k1 - k0);
-    __syncthreads();
-    for (int k = threadIdx.x; k < nt; k += blockDim.x) offs[k] = (size_t)A.col_dn[k0 + k] * du;
-    __syncthreads();
-    for (uint32_t i = r0 + threadIdx.x; i < r1; i += 2 * blockDim.x) {
-      const uint32_t i2 = i + blockDim.x;
-      const bool two = i2 < r1;
-      int64_t a0 = 0, a1 = 0, b0 = 0, b1 = 0;
-      int k = 0;
-#pragma unroll 4
-      for (; k < np; ++k) {
-        a0 += __ldcg(A.x + offs[k] + i);
-        if (two) b0 += __ldcg(A.x + offs[k] + i2);
-      }
-#pragma unroll 4
-      for (; k < nt; ++k) {
-        a1 += __ldcg(A.x + offs[k] + i);
-        if (two) b1 += __ldcg(A.x + offs[k] + i2);
-      }
-      const size_t idx = (size_t)a * du + i;
-      A.y[idx] += mul_fix(a0 - a1, A.mt_dn, A.sh_dn);
-      if (two) A.y[idx + blockDim.x] += mul_fix(b0 - b1, A.mt_dn, A.sh_dn);
-    }
-  }
-}
-
-// Pass D, third form: an item is one row band times a block of kColBlock
-// down states; the neighbour lists of the whole block are staged in shared
-// memory once (one pair of barriers per block instead of per state).
-constexpr int kColBlock = 16;
-constexpr int kMaxDegD = 64;
-
-__global__ void __launch_bounds__(256) k_fx_passD3(FxProdArgs A) {
-  __shared__ uint32_t s_off[kColBlock + 1], s_split[kColBlock];
-  __shared__ size_t s_cols[kColBlock * kMaxDegD];
-  const uint32_t du = A.du, dd = A.dd;
-  const uint32_t nblk = (dd + kColBlock - 1) / kColBlock;
-  const size_t items = (size_t)A.nbands * nblk;
-  for (size_t it = blockIdx.x; it < items; it += gridDim.x) {
-    const uint32_t band = (uint32_t)(it / nblk), blk = (uint32_t)(it % nblk);
-    const uint32_t a0 = blk * kColBlock, a1 = min(dd, a0 + kColBlock);
-    const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
-    const uint32_t base_k = A.rp_dn[a0], total = A.rp_dn[a1] - base_k;
-    __syncthreads();
-    if (threadIdx.x <= a1 - a0) s_off[threadIdx.x] = A.rp_dn[a0 + threadIdx.x] - base_k;
-    if (threadIdx.x < a1 - a0) s_split[threadIdx.x] = A.rs_dn[a0 + threadIdx.x] - base_k;
-    for (uint32_t k = threadIdx.x; k < total; k += blockDim.x)
-      s_cols[k] = (size_t)A.col_dn[base_k + k] * du;
-    __syncthreads();
-    for (uint32_t c = 0; c < a1 - a0; ++c) {
-      const uint32_t k0 = s_off[c], ks = s_split[c], k1 = s_off[c + 1];
-      const size_t ybase = (size_t)(a0 + c) * du;
-      for (uint32_t i = r0 + threadIdx.x; i < r1; i += 2 * blockDim.x) {
-        const uint32_t i2 = i + blockDim.x;
-        const bool two = i2 < r1;
-        const uint32_t j2 = two ? i2 : i;
-        int64_t p0 = 0, n0 = 0, p1 = 0, n1 = 0;
-#pragma unroll 4
-        for (uint32_t k = k0; k < ks; ++k) {
-          const int64_t* col = A.x + s_cols[k];
-          p0 += __ldcg(col + i);
-          p1 += __ldcg(col + j2);
-        }
-#pragma unroll 4
-        for (uint32_t k = ks; k < k1; ++k) {
-          const int64_t* col = A.x + s_cols[k];
-          n0 += __ldcg(col + i);
-          n1 += __ldcg(col + j2);
-        }
-        A.y[ybase + i] += mul_fix(p0 - n0, A.mt_dn, A.sh_dn);
-        if (two) A.y[ybase + i2] += mul_fix(p1 - n1, A.mt_dn, A.sh_dn);
-      }
-    }
-  }
-}
-
 // ---------------------------------------------------------------------------
 // tables
 
@@ -511,33 +235,6 @@ static void build_unit_csr(const HalfOp& op, cudaStream_t s, DevBuf<uint32_t>& r
   QCMG_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
 }
 
-// ELL form of a unit-magnitude CSR (positive hops first per row), 16-bit
-// columns; false when the basis or the degree does not fit the encoding.
-static bool build_ell(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs,
-                      const DevBuf<uint32_t>& col, uint32_t dim, int maxdeg, cudaStream_t s,
-                      DevBuf<uint16_t>& ell, DevBuf<uint16_t>& cnt) {
-  if (dim > 65535u || maxdeg > 32 || dim == 0) return false;
-  std::vector<uint32_t> hrp(dim + 1), hrs(dim);
-  QCMG_CUDA(cudaMemcpyAsync(hrp.data(), rp.p, (dim + 1) * 4, cudaMemcpyDeviceToHost, s));
-  QCMG_CUDA(cudaMemcpyAsync(hrs.data(), rs.p, dim * 4, cudaMemcpyDeviceToHost, s));
-  QCMG_CUDA(cudaStreamSynchronize(s));
-  const size_t nnz = hrp[dim];
-  std::vector<uint32_t> hcol(std::max<size_t>(nnz, 1));
-  if (nnz) QCMG_CUDA(cudaMemcpyAsync(hcol.data(), col.p, nnz * 4, cudaMemcpyDeviceToHost, s));
-  QCMG_CUDA(cudaStreamSynchronize(s));
-  const int md = std::max(maxdeg, 1);
-  std::vector<uint16_t> he((size_t)md * dim, 0), hc(dim);
-  for (uint32_t i = 0; i < dim; ++i) {
-    const uint32_t n = hrp[i + 1] - hrp[i], np = hrs[i] - hrp[i];
-    for (uint32_t k = 0; k < n; ++k) he[(size_t)k * dim + i] = (uint16_t)hcol[hrp[i] + k];
-    hc[i] = (uint16_t)(np | (n << 8));
-  }
-  ell.upload(he.data(), he.size(), s);
-  cnt.upload(hc.data(), hc.size(), s);
-  QCMG_CUDA(cudaStreamSynchronize(s));
-  return true;
-}
-
 __global__ void k_diag_to_fx(const double* __restrict__ d, int64_t* __restrict__ out, size_t n,
                              double scale) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -559,19 +256,9 @@ bool fx_prepare(qcmg_hamiltonian* H) {
   if (!ok) return false;
   build_unit_csr(H->dn, s, T.rp_dn, T.rs_dn, T.col_dn, &T.t_dn, &T.maxdeg_dn, &ok);
   if (!ok) return false;
-  if (T.maxdeg_dn > kMaxDegD) return false;  // pass D stages at most 64 neighbours per state
-  // pass U with bulk-copied slabs: ELL tables and the number of buffers
-  T.nbuf = 0;
-  {
-    const size_t stride = (((size_t)H->du + 2) + 1) & ~(size_t)1;
-    if (H->du >= 64 && build_ell(T.rp_up, T.rs_up, T.col_up, H->du, T.maxdeg_up, s, T.ell_up,
-                                 T.cnt_up)) {
-      if (2 * stride * 8 <= (size_t)max_optin)
-        T.nbuf = 2;
-      else if (stride * 8 <= (size_t)max_optin)
-        T.nbuf = 1;
-    }
-  }
+  // pass U with bulk-copied slabs: grouped ELL table and slabs per round
+  T.ns = choose_slabs_per_pass(H->du, max_optin);
+  if (T.ns > 0 && !build_ell4(T.rp_up, T.rs_up, T.col_up, H->du, s, T.ell4, T.cnt4)) T.ns = 0;
   T.err.alloc(1);
   QCMG_CUDA(cudaMemsetAsync(T.err.p, 0, sizeof(int), s));
   // diagonal bound and fixed-point scale 2^-G
@@ -608,8 +295,10 @@ bool fx_prepare(qcmg_hamiltonian* H) {
   QCMG_CUDA(cudaGetLastError());
   T.bound = dmax + T.t_up * T.maxdeg_up + T.t_dn * T.maxdeg_dn;
   T.b = ceil_log2(std::max(T.bound, 1.0));
-  // rows per band of pass D: ~48 MB of x per band
-  size_t band = (size_t)(48.0e6 / (8.0 * std::max<uint32_t>(H->dd, 1)));
+  // rows per band of pass D: ~48 MB of x per band (QCMG_FX_BAND_MB overrides)
+  double band_mb = 48.0;
+  if (const char* v = std::getenv("QCMG_FX_BAND_MB")) band_mb = std::max(1.0, std::atof(v));
+  size_t band = (size_t)(band_mb * 1.0e6 / (8.0 * std::max<uint32_t>(H->dd, 1)));
   band = std::max<size_t>(256, (band / 256) * 256);
   T.band = (uint32_t)std::min<size_t>(band, H->du);
   T.state = 1;
@@ -704,76 +393,26 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
   split_double(T.t_dn, &A.mt_dn, &e);
   A.sh_dn = Eo - x.E - e;
   A.sh_d = Eo - x.E + T.G;
+  A.p2_up = pow2_exponent(A.mt_up);
+  A.p2_dn = pow2_exponent(A.mt_dn);
   A.yin = nullptr;
   A.m_in = 0;
   A.sh_in = 0;
+  A.p2_in = -1;
   if (yin && yin->mb > 0 && gamma != 0.0) {
     A.yin = yin->buf.p;
     split_double(gamma * yin->c / x.c, &A.m_in, &e);
     A.sh_in = Eo - yin->E - e;
+    A.p2_in = pow2_exponent(A.m_in);
   }
   A.x = x.buf.p;
   A.y = y.buf.p;
   A.band = T.band;
   A.nbands = (H->du + T.band - 1) / T.band;
-  A.ell_up = T.ell_up.p;
-  A.cnt_up = T.cnt_up.p;
-  A.nbuf = T.nbuf;
+  A.ell4 = T.ell4.p;
+  A.cnt4 = T.cnt4.p;
   A.err = T.err.p;
-  // pass U
-  const size_t smem = (size_t)H->du * 8;
-  int max_optin = 0, sms = 0;
-  QCMG_CUDA(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
-  QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
-  QCMG_CHECK_ARG(smem <= (size_t)max_optin, "slab does not fit in shared memory");
-  const int threads = H->du >= 512 ? 512 : (H->du >= 256 ? 256 : 128);
-  const unsigned gU = (unsigned)std::max<size_t>(1, std::min<size_t>(H->dd, (size_t)sms * 2));
-  auto launchU = [&](auto kern) {
-    if (smem > 48 * 1024)
-      QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<gU, threads, smem, s>>>(A);
-  };
-  if (T.nbuf > 0) {
-    const size_t stride = (((size_t)H->du + 2) + 1) & ~(size_t)1;
-    const size_t smem2 = (size_t)T.nbuf * stride * 8;
-    const unsigned g2 = (unsigned)std::max<size_t>(1, std::min<size_t>(H->dd, (size_t)sms));
-    auto launchU2 = [&](auto kern) {
-      QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem2));
-      kern<<<g2, 1024, smem2, s>>>(A);
-    };
-    auto byinter = [&](auto k0, auto k1, auto k2) {
-      switch (H->inter_kind) {
-        case QCMG_INTER_NONE: launchU2(k0); break;
-        case QCMG_INTER_ONSITE: launchU2(k1); break;
-        default: launchU2(k2); break;
-      }
-    };
-    const int md = T.maxdeg_up;
-    if (md <= 8)
-      byinter(k_fx_passU2<QCMG_INTER_NONE, 8>, k_fx_passU2<QCMG_INTER_ONSITE, 8>,
-              k_fx_passU2<QCMG_INTER_GENERAL, 8>);
-    else if (md <= 16)
-      byinter(k_fx_passU2<QCMG_INTER_NONE, 16>, k_fx_passU2<QCMG_INTER_ONSITE, 16>,
-              k_fx_passU2<QCMG_INTER_GENERAL, 16>);
-    else if (md <= 24)
-      byinter(k_fx_passU2<QCMG_INTER_NONE, 24>, k_fx_passU2<QCMG_INTER_ONSITE, 24>,
-              k_fx_passU2<QCMG_INTER_GENERAL, 24>);
-    else
-      byinter(k_fx_passU2<QCMG_INTER_NONE, 32>, k_fx_passU2<QCMG_INTER_ONSITE, 32>,
-              k_fx_passU2<QCMG_INTER_GENERAL, 32>);
-  } else {
-    switch (H->inter_kind) {
-      case QCMG_INTER_NONE: launchU(k_fx_passU<QCMG_INTER_NONE>); break;
-      case QCMG_INTER_ONSITE: launchU(k_fx_passU<QCMG_INTER_ONSITE>); break;
-      default: launchU(k_fx_passU<QCMG_INTER_GENERAL>); break;
-    }
-  }
-  QCMG_CUDA(cudaGetLastError());
-  // pass D
-  const size_t items = (size_t)A.nbands * ((H->dd + kColBlock - 1) / kColBlock);
-  const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>(items, (size_t)sms * 8));
-  k_fx_passD3<<<gD, 256, 0, s>>>(A);
-  QCMG_CUDA(cudaGetLastError());
+  launch_product(H, A, s);
   y.E = Eo;
   y.mb = kFxBits;
   y.c = x.c;

@@ -64,6 +64,20 @@ __device__ __forceinline__ int64_t mul_fix(int64_t a, int64_t m, int s) {
   return shr128_round(mul_s64(a, m), s);
 }
 
+// mul_fix with a multiplier known to be +-2^p when p >= 0 (hop magnitude 1,
+// accumulation factor 1): a shift with the same rounding, bit-identical to
+// mul_fix for |a| < 2^62.  p < 0 falls back to the 128-bit product.
+__device__ __forceinline__ int64_t mul_fix_p2(int64_t a, int64_t m, int s, int p) {
+  if (p >= 0) {
+    const int64_t b = m < 0 ? -a : a;
+    const int t = s - p;
+    if (t <= 0) return (int64_t)((uint64_t)b << (-t));
+    if (t >= 63) return 0;
+    return (b + (1ll << (t - 1))) >> t;
+  }
+  return mul_fix(a, m, s);
+}
+
 // Rounding arithmetic right shift of an int64 (s >= 0; s >= 63 gives 0 or -1 -> 0).
 __device__ __forceinline__ int64_t shr_round(int64_t a, int s) {
   if (s <= 0) return a;

@@ -1,0 +1,487 @@
+// The factorized product y (+)= H x of the fixed-point path.
+//
+// The vector is stored like the reference's (up index fastest: slab a is the
+// du up states of down state a, contiguous).  Two passes:
+//   pass U  persistent CTAs take slabs of x into shared memory with bulk
+//           (TMA) copies; every up-spin hop is an integer gather-add from
+//           the staged slab; the diagonal (one-body diagonal + density-
+//           density terms) and the accumulated input are added; y's slab is
+//           written once.  With room for two slabs, one read of the hop
+//           table serves both.
+//   pass D  one warp per (row band, down state): every down-spin hop adds a
+//           neighbour slab's segment of the band.  Warps sweep the down
+//           states of one band at a time, so the band of x (~48 MB) stays
+//           L2-resident and HBM sees x about once.
+// Restates Hamiltonian_Factorized::mult_add (pyqcm
+// src_ed/Hamiltonian/Hamiltonian_Factorized.hpp:118-170) on fixed-point
+// vectors: hop values share one magnitude per spin (+-t), so a row's hops
+// are a signed sum of gathered entries times t.
+#include <algorithm>
+#include <cstdlib>
+#include <vector>
+
+#include "qcmg_fx.cuh"
+#include "qcmg_fxprod.h"
+#include "qcmg_tma.cuh"
+
+namespace qcmg {
+
+// ---------------------------------------------------------------------------
+// pass U, small slabs: threads stage the slab, hops from the CSR
+
+template <int INTER>
+__global__ void __launch_bounds__(512) k_fx_passU(FxProdArgs A) {
+  extern __shared__ int64_t xs[];
+  const uint32_t du = A.du;
+  for (uint32_t a = blockIdx.x; a < A.dd; a += gridDim.x) {
+    const size_t base = (size_t)a * du;
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < du; i += blockDim.x) xs[i] = A.x[base + i];
+    __syncthreads();
+    const int64_t dda = A.ddn[a];
+    const uint32_t dbits = A.bin_dn[a];
+    for (uint32_t i = threadIdx.x; i < du; i += blockDim.x) {
+      const uint32_t k0 = A.rp_up[i], ks = A.rs_up[i], k1 = A.rp_up[i + 1];
+      int64_t sp = 0, sn = 0;
+      for (uint32_t k = k0; k < ks; ++k) sp += xs[A.col_up[k]];
+      for (uint32_t k = ks; k < k1; ++k) sn += xs[A.col_up[k]];
+      int64_t out = mul_fix(sp - sn, A.mt_up, A.sh_up);
+      int64_t D = A.dup[i] + dda;
+      if (INTER == QCMG_INTER_ONSITE) {
+        D += A.U * (int64_t)__popc(A.bin_up[i] & dbits);
+      } else if (INTER == QCMG_INTER_GENERAL) {
+        uint32_t u = A.bin_up[i];
+        const int64_t* w = A.wdn + (size_t)a * A.L;
+        while (u) {
+          D += w[__ffs(u) - 1];
+          u &= u - 1;
+        }
+      }
+      out += mul_fix(xs[i], D, A.sh_d);
+      if (A.yin) out += mul_fix(A.yin[base + i], A.m_in, A.sh_in);
+      A.y[base + i] = out;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass U, bulk-copied slabs, grouped ELL hops
+
+// Elements per slab buffer: even (16-byte multiple) and at least du + 2, so
+// the zero slot view[du] lies inside the buffer for either view offset.
+__host__ __device__ inline uint32_t slab_stride(uint32_t du) { return (du + 3u) & ~1u; }
+
+// A slab starts at byte a*du*8, which is 8 mod 16 when du and a are odd.
+// The copy moves the 16-byte-aligned interior [e0, e1); thread 0 loads the
+// (at most one) element left over at either end.
+__device__ __forceinline__ void slab_range(uint32_t a, uint32_t du, uint32_t* e0, uint32_t* e1) {
+  const bool odd_start = (du & 1u) && (a & 1u);
+  *e0 = odd_start ? 1u : 0u;
+  *e1 = (du & 1u) ? (odd_start ? du : du - 1u) : du;
+}
+
+// Offset (elements) of the second slab buffer: a compile-time constant, so
+// one address serves the gathers from both slabs.  Two slabs per round need
+// slab_stride(du) <= kSlab1Off (du <= 14205).
+constexpr uint32_t kSlab1Off = 14208;
+
+// Groups of a row whose columns are requested together before the gathers.
+constexpr int kPreGroups = 8;
+
+// 8-byte load from shared memory at a 32-bit address plus a constant offset.
+template <uint32_t OFF>
+__device__ __forceinline__ int64_t lds64(uint32_t addr) {
+  int64_t v;
+  asm volatile("ld.shared.b64 %0, [%1+%2];" : "=l"(v) : "r"(addr), "n"(OFF));
+  return v;
+}
+
+// Sums of the four staged entries named by one group of columns, in each of
+// the NS slabs (the second slab kSlab1Off elements above the first).
+template <int NS>
+__device__ __forceinline__ void gather_group(uint32_t vbase, uint2 w, int64_t (&t)[NS]) {
+  const uint32_t a0 = vbase + ((w.x & 0xffffu) << 3);
+  const uint32_t a1 = vbase + ((w.x >> 16) << 3);
+  const uint32_t a2 = vbase + ((w.y & 0xffffu) << 3);
+  const uint32_t a3 = vbase + ((w.y >> 16) << 3);
+  const int64_t x0 = lds64<0>(a0), x1 = lds64<0>(a1), x2 = lds64<0>(a2), x3 = lds64<0>(a3);
+  if (NS == 2) {
+    constexpr uint32_t O = kSlab1Off * 8;
+    const int64_t y0 = lds64<O>(a0), y1 = lds64<O>(a1), y2 = lds64<O>(a2), y3 = lds64<O>(a3);
+    t[NS - 1] = (y0 + y1) + (y2 + y3);
+  }
+  t[0] = (x0 + x1) + (x2 + x3);
+}
+
+// Each round a CTA stages NS slabs (a, a + G), then every thread takes rows
+// i: one 8-byte load brings four 16-bit hop columns of row i, and each
+// column is gathered from all NS staged slabs.  Row i lists its positive
+// hops in its first groups and its negative hops after them; padding
+// columns point at the zero slot du.  With NS = 2 the grid is even, so the
+// two slabs of a round have the same alignment (view offset).  With NS = 1
+// a second CTA on the SM computes while this one's copy is in flight.
+template <int INTER, int NS>
+__global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_passU4(FxProdArgs A) {
+  extern __shared__ __align__(16) int64_t smem_slab[];
+  __shared__ __align__(8) uint64_t bars[NS];
+  const uint32_t du = A.du, dd = A.dd;
+  const int tid = threadIdx.x;
+  const uint32_t G = gridDim.x;
+  if (NS == 2 && (G & 1u)) {  // launch contract: even grid
+    if (tid == 0 && blockIdx.x == 0) atomicExch(A.err, 1);
+    return;
+  }
+  if (tid == 0) {
+#pragma unroll
+    for (int s = 0; s < NS; ++s) mbar_init(&bars[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  unsigned parity = 0u;
+  for (uint32_t a0 = blockIdx.x; a0 < dd; a0 += NS * G) {
+    if (tid == 0) {
+      fence_proxy_async_smem();  // earlier generic accesses before the copies
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        const uint32_t a = a0 + s * G;
+        if (a >= dd) break;
+        uint32_t e0, e1;
+        slab_range(a, du, &e0, &e1);
+        const unsigned bytes = (e1 - e0) * 8u;
+        mbar_arrive_expect_tx(&bars[s], bytes);
+        bulk_g2s(smem_slab + s * kSlab1Off + 2 * e0, A.x + (size_t)a * du + e0, bytes, &bars[s]);
+      }
+    }
+    bool ok = true;
+#pragma unroll
+    for (int s = 0; s < NS; ++s)
+      if (a0 + s * G < dd) ok = mbar_wait_bounded(&bars[s], parity) && ok;
+    if (__syncthreads_or(!ok)) {  // CTA-uniform decision: every thread leaves together
+      if (tid == 0) {
+        atomicExch(A.err, 1);
+        // give copies still in flight a last bounded chance to land
+#pragma unroll
+        for (int s = 0; s < NS; ++s)
+          if (a0 + s * G < dd) (void)mbar_wait_bounded(&bars[s], parity);
+      }
+      return;
+    }
+    parity ^= 1u;
+    // element j of slab s is view[s * kSlab1Off + j]; the copy landed at
+    // buf + 2*e0, so view = buf + e0 (e0 is the same for both slabs).
+    uint32_t e0, e1;
+    slab_range(a0, du, &e0, &e1);
+    const int64_t* view = smem_slab + e0;
+    int64_t dda[NS];
+    uint32_t dbits[NS];
+#pragma unroll
+    for (int s = 0; s < NS; ++s) {
+      const uint32_t a = min(a0 + s * G, dd - 1u);
+      dda[s] = A.ddn[a];
+      dbits[s] = A.bin_dn[a];
+      if (tid == 0 && a0 + s * G < dd) {
+        int64_t* v = smem_slab + s * kSlab1Off + e0;
+        const size_t base = (size_t)a * du;
+        if (e0 == 1u) v[0] = A.x[base];
+        if (e1 == du - 1u) v[du - 1] = A.x[base + du - 1];
+        v[du] = 0;  // zero slot for padding columns
+      }
+    }
+    __syncthreads();
+    const uint32_t vbase = smem_u32(view);
+    const uint32_t bd = blockDim.x;
+    // the next row's group counts are loaded one row ahead; a row's group
+    // columns, diagonal and accumulated input are all requested before its
+    // first gather
+    uint32_t c_next = tid < du ? __ldg(A.cnt4 + tid) : 0u;
+    for (uint32_t i = tid; i < du; i += bd) {
+      const uint32_t c = c_next;
+      const uint32_t gp = c & 0xffu, gt = gp + (c >> 8);
+      uint2 w[kPreGroups];
+#pragma unroll
+      for (int g = 0; g < kPreGroups; ++g)
+        w[g] = ((uint32_t)g < gt) ? __ldg(A.ell4 + (size_t)g * du + i) : make_uint2(0u, 0u);
+      const int64_t dui = __ldg(A.dup + i);
+      const uint32_t ubits = __ldg(A.bin_up + i);
+      int64_t yv[NS];
+#pragma unroll
+      for (int s = 0; s < NS; ++s)
+        yv[s] = (A.yin && a0 + s * G < dd) ? __ldcs(A.yin + (size_t)(a0 + s * G) * du + i) : 0;
+      if (i + bd < du) c_next = __ldg(A.cnt4 + i + bd);
+      int64_t sp[NS], sn[NS];
+#pragma unroll
+      for (int s = 0; s < NS; ++s) sp[s] = sn[s] = 0;
+#pragma unroll
+      for (int g = 0; g < kPreGroups; ++g) {
+        if ((uint32_t)g < gt) {
+          int64_t t[NS];
+          gather_group<NS>(vbase, w[g], t);
+#pragma unroll
+          for (int s = 0; s < NS; ++s) {
+            if ((uint32_t)g < gp)
+              sp[s] += t[s];
+            else
+              sn[s] += t[s];
+          }
+        }
+      }
+      for (uint32_t g = kPreGroups; g < gt; ++g) {  // rows with more than kPreGroups groups
+        int64_t t[NS];
+        gather_group<NS>(vbase, __ldg(A.ell4 + (size_t)g * du + i), t);
+#pragma unroll
+        for (int s = 0; s < NS; ++s) {
+          if (g < gp)
+            sp[s] += t[s];
+          else
+            sn[s] += t[s];
+        }
+      }
+#pragma unroll
+      for (int s = 0; s < NS; ++s) {
+        const uint32_t a = a0 + s * G;
+        if (a >= dd) break;
+        const size_t base = (size_t)a * du;
+        int64_t out = mul_fix_p2(sp[s] - sn[s], A.mt_up, A.sh_up, A.p2_up);
+        int64_t D = dui + dda[s];
+        if (INTER == QCMG_INTER_ONSITE) {
+          D += A.U * (int64_t)__popc(ubits & dbits[s]);
+        } else if (INTER == QCMG_INTER_GENERAL) {
+          uint32_t u = ubits;
+          const int64_t* wt = A.wdn + (size_t)a * A.L;
+          while (u) {
+            D += wt[__ffs(u) - 1];
+            u &= u - 1;
+          }
+        }
+        out += mul_fix(view[s * kSlab1Off + i], D, A.sh_d);
+        if (A.yin) out += mul_fix_p2(yv[s], A.m_in, A.sh_in, A.p2_in);
+        __stcs(A.y + base + i, out);
+      }
+    }
+    __syncthreads();  // every buffer is free again
+  }
+}
+
+// ---------------------------------------------------------------------------
+// pass D: one warp per (band, down state)
+
+// Adds, for the neighbours k in [kf, kt) of the current chunk (columns held
+// one per lane in ccol), the band segments at rows ia.. and ib.. (VEC
+// consecutive elements each) into acc.
+template <int VEC>
+__device__ __forceinline__ void passD_accum(const int64_t* __restrict__ x, uint32_t du,
+                                            uint32_t ccol, uint32_t kf, uint32_t kt, uint32_t ia,
+                                            uint32_t ib, bool va, bool vb, int64_t (&acc)[2 * VEC]) {
+#pragma unroll 4
+  for (uint32_t k = kf; k < kt; ++k) {
+    const uint32_t b = __shfl_sync(0xffffffffu, ccol, (int)k);
+    const int64_t* src = x + (size_t)b * du;
+    if (VEC == 2) {
+      if (va) {
+        const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(src + ia));
+        acc[0] += v.x;
+        acc[1] += v.y;
+      }
+      if (vb) {
+        const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(src + ib));
+        acc[2] += v.x;
+        acc[3] += v.y;
+      }
+    } else {
+      if (va) acc[0] += __ldcg(src + ia);
+      if (vb) acc[1] += __ldcg(src + ib);
+    }
+  }
+}
+
+// VEC = 2 needs du even (every slab segment at an even row is 16-byte
+// aligned); bands start at multiples of 256 rows.
+template <int VEC>
+__global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
+  const uint32_t du = A.du, dd = A.dd;
+  const uint32_t lane = threadIdx.x & 31u;
+  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
+  const size_t items = (size_t)A.nbands * dd;
+  constexpr uint32_t kSweep = 64u * VEC;  // rows per warp sweep: two VEC-chunks per lane
+  for (size_t it = warp; it < items; it += nwarps) {
+    const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
+    const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
+    const uint32_t k0 = A.rp_dn[a], np = A.rs_dn[a] - k0, nt = A.rp_dn[a + 1] - k0;
+    int64_t* yrow = A.y + (size_t)a * du;
+    for (uint32_t i0 = r0; i0 < r1; i0 += kSweep) {
+      const uint32_t ia = i0 + lane * VEC, ib = ia + 32u * VEC;
+      const bool va = ia < r1, vb = ib < r1;
+      int64_t P[2 * VEC], N[2 * VEC];
+#pragma unroll
+      for (int e = 0; e < 2 * VEC; ++e) P[e] = N[e] = 0;
+      for (uint32_t kc = 0; kc < nt; kc += 32u) {
+        const uint32_t ccol = (kc + lane < nt) ? A.col_dn[k0 + kc + lane] : 0u;
+        const uint32_t e = min(32u, nt - kc);
+        const uint32_t spos = np > kc ? min(e, np - kc) : 0u;
+        passD_accum<VEC>(A.x, du, ccol, 0u, spos, ia, ib, va, vb, P);
+        passD_accum<VEC>(A.x, du, ccol, spos, e, ia, ib, va, vb, N);
+      }
+      // y streams through once (evict-first), leaving L2 to the band of x
+      const int64_t m = A.mt_dn;
+      const int sh = A.sh_dn, p2 = A.p2_dn;
+      if (VEC == 2) {
+        if (va) {
+          longlong2* yp = reinterpret_cast<longlong2*>(yrow + ia);
+          longlong2 v = __ldcs(yp);
+          v.x += mul_fix_p2(P[0] - N[0], m, sh, p2);
+          v.y += mul_fix_p2(P[1] - N[1], m, sh, p2);
+          __stcs(yp, v);
+        }
+        if (vb) {
+          longlong2* yp = reinterpret_cast<longlong2*>(yrow + ib);
+          longlong2 v = __ldcs(yp);
+          v.x += mul_fix_p2(P[2] - N[2], m, sh, p2);
+          v.y += mul_fix_p2(P[3] - N[3], m, sh, p2);
+          __stcs(yp, v);
+        }
+      } else {
+        if (va) __stcs(yrow + ia, __ldcs(yrow + ia) + mul_fix_p2(P[0] - N[0], m, sh, p2));
+        if (vb) __stcs(yrow + ib, __ldcs(yrow + ib) + mul_fix_p2(P[1] - N[1], m, sh, p2));
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// tables
+
+// Grouped ELL: row i holds ceil(np/4) groups of its positive hop columns,
+// then ceil(nn/4) groups of its negative ones, four 16-bit columns per
+// group, padded with dim (the zero slot behind each staged slab);
+// ell4[g * dim + i] is group g of row i and cnt4[i] = positive groups |
+// (negative groups << 8).
+bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const DevBuf<uint32_t>& col,
+                uint32_t dim, cudaStream_t s, DevBuf<uint2>& ell4, DevBuf<uint16_t>& cnt4) {
+  if (dim == 0 || dim > 65534u) return false;
+  std::vector<uint32_t> hrp(dim + 1), hrs(dim);
+  QCMG_CUDA(cudaMemcpyAsync(hrp.data(), rp.p, (dim + 1) * 4, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaMemcpyAsync(hrs.data(), rs.p, dim * 4, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaStreamSynchronize(s));
+  const size_t nnz = hrp[dim];
+  std::vector<uint32_t> hcol(std::max<size_t>(nnz, 1));
+  if (nnz) QCMG_CUDA(cudaMemcpyAsync(hcol.data(), col.p, nnz * 4, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaStreamSynchronize(s));
+  uint32_t groups = 1;
+  for (uint32_t i = 0; i < dim; ++i) {
+    const uint32_t np = hrs[i] - hrp[i], nn = hrp[i + 1] - hrs[i];
+    const uint32_t gp = (np + 3) / 4, gn = (nn + 3) / 4;
+    if (gp > 255 || gn > 255) return false;
+    groups = std::max(groups, gp + gn);
+  }
+  const uint16_t Z = (uint16_t)dim;
+  std::vector<uint16_t> cols((size_t)groups * 4 * dim, Z), hc(dim);
+  // cols is laid out as [group][row][4]; each sign list is sorted, so the
+  // k-th columns of neighbouring rows tend to be close (fewer shared-memory
+  // bank conflicts between the lanes of a warp)
+  std::vector<uint32_t> tmp;
+  for (uint32_t i = 0; i < dim; ++i) {
+    const uint32_t np = hrs[i] - hrp[i], nn = hrp[i + 1] - hrs[i];
+    const uint32_t gp = (np + 3) / 4, gn = (nn + 3) / 4;
+    tmp.assign(hcol.begin() + hrp[i], hcol.begin() + hrs[i]);
+    std::sort(tmp.begin(), tmp.end());
+    for (uint32_t k = 0; k < np; ++k) cols[((size_t)(k / 4) * dim + i) * 4 + (k % 4)] = (uint16_t)tmp[k];
+    tmp.assign(hcol.begin() + hrs[i], hcol.begin() + hrp[i + 1]);
+    std::sort(tmp.begin(), tmp.end());
+    for (uint32_t k = 0; k < nn; ++k)
+      cols[((size_t)(gp + k / 4) * dim + i) * 4 + (k % 4)] = (uint16_t)tmp[k];
+    hc[i] = (uint16_t)(gp | (gn << 8));
+  }
+  std::vector<uint2> he((size_t)groups * dim);
+  for (size_t q = 0; q < he.size(); ++q) {
+    he[q].x = (uint32_t)cols[4 * q] | ((uint32_t)cols[4 * q + 1] << 16);
+    he[q].y = (uint32_t)cols[4 * q + 2] | ((uint32_t)cols[4 * q + 3] << 16);
+  }
+  ell4.upload(he.data(), he.size(), s);
+  cnt4.upload(hc.data(), hc.size(), s);
+  QCMG_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+  return true;
+}
+
+int pow2_exponent(int64_t m) {
+  if (m == 0 || m == INT64_MIN) return -1;
+  const uint64_t a = (uint64_t)(m < 0 ? -m : m);
+  if (a & (a - 1)) return -1;
+  int p = 0;
+  while ((1ull << p) != a) ++p;
+  return p;
+}
+
+int choose_slabs_per_pass(uint32_t du, int max_optin_smem) {
+  if (du < 64 || du > 65534u) return 0;
+  const size_t one = (size_t)slab_stride(du) * 8;
+  if (one > (size_t)max_optin_smem) return 0;
+  const bool two_fit = slab_stride(du) <= kSlab1Off &&
+                       ((size_t)kSlab1Off + slab_stride(du)) * 8 <= (size_t)max_optin_smem;
+  int ns = two_fit ? 2 : 1;
+  if (const char* e = std::getenv("QCMG_FX_SLABS")) {
+    const int v = std::atoi(e);
+    if (v == 1) ns = 1;
+    if (v == 2 && two_fit) ns = 2;
+  }
+  return ns;
+}
+
+// ---------------------------------------------------------------------------
+// launcher
+
+template <int NS, typename Kern>
+static void launch_passU4(Kern kern, const qcmg_hamiltonian* H, const FxProdArgs& A, int sms,
+                          cudaStream_t s) {
+  const size_t smem = ((NS == 2 ? (size_t)kSlab1Off : 0) + slab_stride(H->du)) * 8;
+  QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int tmax = NS == 1 ? 512 : 1024;
+  const int threads = std::min<int>(tmax, (int)((H->du + 127) / 128 * 128));
+  int per_sm = 0;
+  QCMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem));
+  per_sm = std::max(per_sm, 1);
+  const size_t rounds = ((size_t)H->dd + NS - 1) / NS;
+  size_t grid = std::max<size_t>(1, std::min<size_t>(rounds, (size_t)sms * per_sm));
+  if (NS == 2 && (grid & 1)) ++grid;  // even: the two slabs of a round share their alignment
+  kern<<<(unsigned)grid, threads, smem, s>>>(A);
+}
+
+void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s) {
+  const FxTables& T = H->fx;
+  int sms = 0;
+  QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
+  const int ik = H->inter_kind;
+  // pass U
+  if (T.ns == 2) {
+    if (ik == QCMG_INTER_NONE) launch_passU4<2>(k_fx_passU4<QCMG_INTER_NONE, 2>, H, A, sms, s);
+    else if (ik == QCMG_INTER_ONSITE) launch_passU4<2>(k_fx_passU4<QCMG_INTER_ONSITE, 2>, H, A, sms, s);
+    else launch_passU4<2>(k_fx_passU4<QCMG_INTER_GENERAL, 2>, H, A, sms, s);
+  } else if (T.ns == 1) {
+    if (ik == QCMG_INTER_NONE) launch_passU4<1>(k_fx_passU4<QCMG_INTER_NONE, 1>, H, A, sms, s);
+    else if (ik == QCMG_INTER_ONSITE) launch_passU4<1>(k_fx_passU4<QCMG_INTER_ONSITE, 1>, H, A, sms, s);
+    else launch_passU4<1>(k_fx_passU4<QCMG_INTER_GENERAL, 1>, H, A, sms, s);
+  } else {
+    const size_t smem = (size_t)H->du * 8;
+    const int threads = H->du >= 512 ? 512 : (H->du >= 256 ? 256 : 128);
+    const unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>(H->dd, (size_t)sms * 2));
+    auto go = [&](auto kern) {
+      if (smem > 48 * 1024)
+        QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+      kern<<<g, threads, smem, s>>>(A);
+    };
+    if (ik == QCMG_INTER_NONE) go(k_fx_passU<QCMG_INTER_NONE>);
+    else if (ik == QCMG_INTER_ONSITE) go(k_fx_passU<QCMG_INTER_ONSITE>);
+    else go(k_fx_passU<QCMG_INTER_GENERAL>);
+  }
+  QCMG_CUDA(cudaGetLastError());
+  // pass D
+  const size_t items = (size_t)A.nbands * H->dd;
+  const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * 8));
+  if ((H->du & 1u) == 0u)
+    k_fx_passD4<2><<<gD, 256, 0, s>>>(A);
+  else
+    k_fx_passD4<1><<<gD, 256, 0, s>>>(A);
+  QCMG_CUDA(cudaGetLastError());
+}
+
+}  // namespace qcmg

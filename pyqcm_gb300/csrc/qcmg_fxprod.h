@@ -1,0 +1,62 @@
+// Factorized product kernels of the fixed-point path: arguments, tables and
+// the launcher (qcmg_fxprod.cu).
+#pragma once
+
+#include <cstdint>
+
+#include "qcmg_internal.h"
+
+namespace qcmg {
+
+struct FxProdArgs {
+  uint32_t du, dd;
+  int L;
+  // up half-operator: row i has positive hops cols[rp[i]..rs[i]) and negative
+  // hops cols[rs[i]..rp[i+1]) (used for slabs too small to bulk-copy)
+  const uint32_t* rp_up;
+  const uint32_t* rs_up;
+  const uint32_t* col_up;
+  const uint32_t* rp_dn;
+  const uint32_t* rs_dn;
+  const uint32_t* col_dn;
+  const int64_t* dup;  // fixed-point diagonal of each half basis (scale 2^-G)
+  const int64_t* ddn;
+  const uint32_t* bin_up;
+  const uint32_t* bin_dn;
+  int64_t U;           // on-site interaction (scale 2^-G)
+  const int64_t* wdn;  // dd x L cross table (scale 2^-G), general interactions
+  int64_t mt_up, mt_dn;  // hop magnitudes (mantissas)
+  int sh_up, sh_dn;      // shifts of the hop terms
+  int p2_up, p2_dn;      // log2 |mt| when |mt| is a power of two, else -1
+  int sh_d;              // shift of the diagonal term
+  const int64_t* yin;    // accumulated input (may alias y) or null
+  int64_t m_in;
+  int sh_in;
+  int p2_in;
+  const int64_t* x;
+  int64_t* y;
+  uint32_t band;  // rows per band (pass D)
+  uint32_t nbands;
+  // grouped ELL form of the up half-operator (see build_ell4)
+  const uint2* ell4;
+  const uint16_t* cnt4;
+  int* err;  // set to 1 when a bounded wait gives up
+};
+
+// Builds the grouped ELL form of the up-spin hops from the unit-magnitude
+// CSR (positive hops first in each row).  False when the half basis is too
+// large for 16-bit columns.
+bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const DevBuf<uint32_t>& col,
+                uint32_t dim, cudaStream_t s, DevBuf<uint2>& ell4, DevBuf<uint16_t>& cnt4);
+
+// Slabs staged per table read by pass U: 1 or 2 (0 when the slab is not
+// bulk-copied).  QCMG_FX_SLABS=1|2 overrides the choice.
+int choose_slabs_per_pass(uint32_t du, int max_optin_smem);
+
+// log2 |m| when |m| is a power of two, else -1 (for FxProdArgs::p2_*).
+int pow2_exponent(int64_t m);
+
+// Launches pass U then pass D for y (+)= H x.
+void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s);
+
+}  // namespace qcmg

@@ -134,8 +134,9 @@ struct FxTables {
   double bound = 0.0;  // bound on |H|_inf
   int b = 0;
   uint32_t band = 0;  // rows per band of the down-spin pass
-  DevBuf<uint16_t> ell_up, cnt_up;  // ELL form of the up hops (pass U with bulk copies)
-  int nbuf = 0;                     // 0: shared-memory staging by threads; 1-2: bulk-copy buffers
+  DevBuf<uint2> ell4;     // grouped ELL form of the up hops (pass U with bulk copies)
+  DevBuf<uint16_t> cnt4;  // groups per row of ell4
+  int ns = 0;             // slabs per pass U round: 0 (threads stage the slab), 1 or 2
   DevBuf<int> err;                  // bounded-wait failure flag of the kernels
   FxVec x, y;         // staging of the FP64-interface product
   DevBuf<unsigned long long> tmp;

@@ -193,11 +193,12 @@ class Hamiltonian:
         check(lib().qcmg_hamiltonian_fx_available(self._h, a))
         return bool(a.value)
 
-    def matvec_fx_device(self, qx_ptr, Ex, mbx, qy_ptr, asynchronous=False):
-        """y = H x on fixed-point device vectors; returns the exponent of y."""
-        Ey = _lib.c_int()
-        check(lib().qcmg_matvec_fx(self._h, qx_ptr, Ex, mbx, qy_ptr, Ey,
-                                   _lib.QCMG_ASYNC if asynchronous else 0))
+    def matvec_fx_device(self, qx_ptr, Ex, mbx, qy_ptr, asynchronous=False, Ey_in=None):
+        """y = H x on fixed-point device vectors (y = y + H x when Ey_in, the
+        exponent of the input y, is given); returns the exponent of y."""
+        Ey = _lib.c_int(0 if Ey_in is None else Ey_in)
+        flags = (_lib.QCMG_ASYNC if asynchronous else 0) | (0 if Ey_in is None else _lib.QCMG_ACCUMULATE)
+        check(lib().qcmg_matvec_fx(self._h, qx_ptr, Ex, mbx, qy_ptr, Ey, flags))
         return Ey.value
 
     def halfop(self, spin):

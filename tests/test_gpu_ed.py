@@ -191,6 +191,34 @@ def test_fixed_point_product_matches_reference(pg, tag):
     assert np.max(np.abs(y2 - 0.25 - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("slabs", ["1", "2"])
+@pytest.mark.parametrize("shape,n", [((4, 3), 12), ((13, 1), 10)])
+def test_fixed_point_product_slab_variants(pg, monkeypatch, slabs, shape, n):
+    """Pass U with one and two slabs per round, on an even half basis (4x3,
+    du = 924: 16-byte pass D loads) and an odd one (13-site chain, 5+5
+    electrons, du = 1287: split bulk copies, 8-byte pass D loads), against
+    the oracle on the same seeded vector."""
+    import models
+    monkeypatch.setenv("QCMG_FX_SLABS", slabs)
+    ns, nb, ops = models.hubbard_cluster(*shape)
+    params = {"t": 1.0, "U": 8.0, "mu": 4.0}
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        if name in params:
+            m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, params, f"R0:N{n}:S0")
+    assert H.fx_available()
+    up, dn, pr = qo.combine_terms({k: v for k, v in ops.items() if k in params}, params, ns)
+    S = qo.Sector(ns, n // 2, n // 2, up, dn, pr)
+    x = qo.seeded_start(H.dim, 5)
+    ref = S.matvec(x, nthreads=8)
+    y = H.matvec(x)
+    assert np.max(np.abs(y - ref)) <= 1e-13 * np.max(np.abs(ref))
+    y2 = np.full(H.dim, -0.5)
+    H.mult_add(x, y2)
+    assert np.max(np.abs(y2 + 0.5 - ref)) <= 1e-13 * np.max(np.abs(ref))
+
+
 def test_fixed_point_not_used_for_mixed_hops(pg):
     m, params, sec = engine_model("ladder2x4_af")  # t and t' differ
     H = pg.Hamiltonian(m, params, sec)
@@ -218,6 +246,31 @@ def test_fixed_point_conversion_roundtrip(pg):
     assert err <= 2.0 ** (E.value - 1) * 1.0000001
     assert err <= 2.0 ** -55 * float(x.abs().max())
     assert float(back[7]) == 0.0
+
+
+def test_fixed_point_device_accumulate(pg):
+    """qcmg_matvec_fx with QCMG_ACCUMULATE: y <- y + H x on device
+    fixed-point vectors, against y0 + the reference's product (chain8)."""
+    torch = _torch()
+    from pyqcm_gb300 import _lib
+    g = load_golden("chain8")
+    m, params, sec = engine_model("chain8")
+    H = pg.Hamiltonian(m, params, sec)
+    x = torch.tensor(g["h_x0"], dtype=torch.float64, device="cuda")
+    y0 = torch.linspace(-1.0, 1.0, H.dim, dtype=torch.float64, device="cuda")
+    qx = torch.empty(H.dim, dtype=torch.int64, device="cuda")
+    qy = torch.empty_like(qx)
+    Ex, mbx, Ey, mby = _lib.c_int(), _lib.c_int(), _lib.c_int(), _lib.c_int()
+    _lib.check(pg.lib().qcmg_fx_from_f64(H.dim, x.data_ptr(), qx.data_ptr(), Ex, mbx, None))
+    _lib.check(pg.lib().qcmg_fx_from_f64(H.dim, y0.data_ptr(), qy.data_ptr(), Ey, mby, None))
+    e = Ey.value
+    for _ in range(2):  # two accumulations in a row
+        e = H.matvec_fx_device(qx.data_ptr(), Ex.value, mbx.value, qy.data_ptr(), Ey_in=e)
+    y = torch.empty_like(x)
+    _lib.check(pg.lib().qcmg_fx_to_f64(H.dim, qy.data_ptr(), e, y.data_ptr(), None))
+    torch.cuda.synchronize()
+    ref = y0.cpu().numpy() + 2.0 * g["h_Hx0"]
+    assert np.max(np.abs(y.cpu().numpy() - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
 def test_fixed_point_product_4x4_full_sector(pg):
