@@ -146,6 +146,19 @@ int qcmg_matvec_fx(qcmg_hamiltonian* H, const int64_t* qx, int Ex, int mbx, int6
 int qcmg_multidot(int m, const double* const* V, const double* w, size_t n, double* out,
                   void* stream);
 
+/* qcmg_multidot for callers that may not allocate device memory (a host
+ * framework owning the GPU through its own pool or a memory cap; code that
+ * must not allocate while other work runs).  No counterpart in the
+ * reference.  Same arguments and kernels, except that out is a DEVICE array
+ * of m doubles and the call returns without waiting.  Allocates nothing:
+ * the partial sums live in a fixed 155,648-byte device array of the library,
+ * so m is limited to 64 (QCMG_ERR_ARG beyond).  The first call on a device
+ * (with that device current) looks up that array's address; make it before
+ * any stream capture.  Calls that overlap in time on one device race on the
+ * array: serialize them. */
+int qcmg_multidot_noalloc(int m, const double* const* V, const double* w, size_t n, double* out,
+                          void* stream);
+
 /* Seeded start vector of the reference: std::default_random_engine(seed)
  * drawing std::normal_distribution(0,1), normalized.
  * Replaces random() (src_util/vector_num.cpp:114-119). */

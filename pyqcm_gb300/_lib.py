@@ -53,6 +53,7 @@ SIGNATURES = {
     "qcmg_fx_to_f64": (c_int, [c_size_t, vp, c_int, vp, vp]),
     "qcmg_matvec_fx": (c_int, [vp, vp, c_int, c_int, vp, int_p, c_uint]),
     "qcmg_multidot": (c_int, [c_int, vp, vp, c_size_t, vp, vp]),
+    "qcmg_multidot_noalloc": (c_int, [c_int, vp, vp, c_size_t, vp, vp]),
     "qcmg_seeded_vector": (c_int, [c_size_t, c_uint, vp]),
     "qcmg_lanczos_ground_state": (c_int, [vp, vp, c_uint, c_double, c_int, c_int, dbl_p, vp,
                                           int_p, vp, vp, c_int]),
