@@ -293,6 +293,23 @@ bool fx_prepare(qcmg_hamiltonian* H) {
     k_diag_to_fx<<<grid_ew(hw.size()), 256, 0, s>>>(H->wdn.p, T.wdn.p, hw.size(), scale);
   }
   QCMG_CUDA(cudaGetLastError());
+  // Narrow diagonal: when every diagonal entry at scale 2^-G is a multiple of
+  // 2^tz and |D| >> tz stays below 2^6 (small-integer energies such as the
+  // Hubbard model's), x * (D >> tz) fits in 63 bits and the diagonal term is
+  // one 64-bit product and a rounding shift, bit-identical to the 128-bit one.
+  {
+    int tz = 63;
+    auto fold = [&](double v) {
+      const long long q = std::llrint(v * scale);  // the value k_diag_to_fx stores
+      if (q != 0) tz = std::min(tz, __builtin_ctzll((unsigned long long)q));
+    };
+    for (double v : hdu) fold(v);
+    for (double v : hdd) fold(v);
+    for (double v : hw) fold(v);
+    if (H->inter_kind == QCMG_INTER_ONSITE) fold(H->U);
+    const double dbound = std::ceil(dmax * scale);
+    T.dtz = (std::ldexp(dbound, -tz) < 64.0) ? tz : -1;
+  }
   T.bound = dmax + T.t_up * T.maxdeg_up + T.t_dn * T.maxdeg_dn;
   T.b = ceil_log2(std::max(T.bound, 1.0));
   // rows per band of pass D: ~48 MB of x per band (QCMG_FX_BAND_MB overrides)
@@ -393,6 +410,7 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
   split_double(T.t_dn, &A.mt_dn, &e);
   A.sh_dn = Eo - x.E - e;
   A.sh_d = Eo - x.E + T.G;
+  A.d_tz = T.dtz;
   A.p2_up = pow2_exponent(A.mt_up);
   A.p2_dn = pow2_exponent(A.mt_dn);
   A.yin = nullptr;

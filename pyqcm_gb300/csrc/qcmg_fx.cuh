@@ -67,15 +67,25 @@ __device__ __forceinline__ int64_t mul_fix(int64_t a, int64_t m, int s) {
 // mul_fix with a multiplier known to be +-2^p when p >= 0 (hop magnitude 1,
 // accumulation factor 1): a shift with the same rounding, bit-identical to
 // mul_fix for |a| < 2^62.  p < 0 falls back to the 128-bit product.
+// round(v / 2^t) with mul_fix's rounding, for |v| < 2^62 (t <= 0: v * 2^-t).
+__device__ __forceinline__ int64_t round_shift(int64_t v, int t) {
+  if (t <= 0) return (int64_t)((uint64_t)v << (-t));
+  if (t >= 63) return 0;
+  return (v + (1ll << (t - 1))) >> t;
+}
+
 __device__ __forceinline__ int64_t mul_fix_p2(int64_t a, int64_t m, int s, int p) {
-  if (p >= 0) {
-    const int64_t b = m < 0 ? -a : a;
-    const int t = s - p;
-    if (t <= 0) return (int64_t)((uint64_t)b << (-t));
-    if (t >= 63) return 0;
-    return (b + (1ll << (t - 1))) >> t;
-  }
+  if (p >= 0) return round_shift(m < 0 ? -a : a, s - p);
   return mul_fix(a, m, s);
+}
+
+// The diagonal term round(x * D / 2^s).  tz >= 0 means D is a multiple of
+// 2^tz with |D >> tz| < 2^6, so x * (D >> tz) fits in 63 bits and one 64-bit
+// product replaces the 128-bit one (bit-identical result); tz < 0 takes the
+// 128-bit product.
+__device__ __forceinline__ int64_t mul_fix_diag(int64_t x, int64_t D, int s, int tz) {
+  if (tz >= 0) return round_shift(x * (D >> tz), s - tz);
+  return mul_fix(x, D, s);
 }
 
 // Rounding arithmetic right shift of an int64 (s >= 0; s >= 63 gives 0 or -1 -> 0).

@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(512) k_fx_passU(FxProdArgs A) {
           u &= u - 1;
         }
       }
-      out += mul_fix(xs[i], D, A.sh_d);
+      out += mul_fix_diag(xs[i], D, A.sh_d, A.d_tz);
       if (A.yin) out += mul_fix(A.yin[base + i], A.m_in, A.sh_in);
       A.y[base + i] = out;
     }
@@ -86,7 +86,7 @@ __device__ __forceinline__ void slab_range(uint32_t a, uint32_t du, uint32_t* e0
 constexpr uint32_t kSlab1Off = 14208;
 
 // Groups of a row whose columns are requested together before the gathers.
-constexpr int kPreGroups = 8;
+constexpr int kPreGroups = 4;
 
 // 8-byte load from shared memory at a 32-bit address plus a constant offset.
 template <uint32_t OFF>
@@ -197,10 +197,11 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
     for (uint32_t i = tid; i < du; i += bd) {
       const uint32_t c = c_next;
       const uint32_t gp = c & 0xffu, gt = gp + (c >> 8);
+      // the table holds at least kPreGroups groups per row (zero-slot padding),
+      // so the first ones are loaded and gathered without a per-row test
       uint2 w[kPreGroups];
 #pragma unroll
-      for (int g = 0; g < kPreGroups; ++g)
-        w[g] = ((uint32_t)g < gt) ? __ldg(A.ell4 + (size_t)g * du + i) : make_uint2(0u, 0u);
+      for (int g = 0; g < kPreGroups; ++g) w[g] = __ldg(A.ell4 + (size_t)g * du + i);
       const int64_t dui = __ldg(A.dup + i);
       const uint32_t ubits = __ldg(A.bin_up + i);
       int64_t yv[NS];
@@ -213,16 +214,14 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
       for (int s = 0; s < NS; ++s) sp[s] = sn[s] = 0;
 #pragma unroll
       for (int g = 0; g < kPreGroups; ++g) {
-        if ((uint32_t)g < gt) {
-          int64_t t[NS];
-          gather_group<NS>(vbase, w[g], t);
+        int64_t t[NS];
+        gather_group<NS>(vbase, w[g], t);
 #pragma unroll
-          for (int s = 0; s < NS; ++s) {
-            if ((uint32_t)g < gp)
-              sp[s] += t[s];
-            else
-              sn[s] += t[s];
-          }
+        for (int s = 0; s < NS; ++s) {
+          if ((uint32_t)g < gp)
+            sp[s] += t[s];
+          else
+            sn[s] += t[s];
         }
       }
       for (uint32_t g = kPreGroups; g < gt; ++g) {  // rows with more than kPreGroups groups
@@ -253,7 +252,7 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
             u &= u - 1;
           }
         }
-        out += mul_fix(view[s * kSlab1Off + i], D, A.sh_d);
+        out += mul_fix_diag(view[s * kSlab1Off + i], D, A.sh_d, A.d_tz);
         if (A.yin) out += mul_fix_p2(yv[s], A.m_in, A.sh_in, A.p2_in);
         __stcs(A.y + base + i, out);
       }
@@ -374,6 +373,7 @@ bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const De
     if (gp > 255 || gn > 255) return false;
     groups = std::max(groups, gp + gn);
   }
+  groups = std::max<uint32_t>(groups, kPreGroups);  // pass U loads the first kPreGroups unconditionally
   const uint16_t Z = (uint16_t)dim;
   std::vector<uint16_t> cols((size_t)groups * 4 * dim, Z), hc(dim);
   // cols is laid out as [group][row][4]; each sign list is sorted, so the

@@ -29,6 +29,7 @@ struct FxProdArgs {
   int sh_up, sh_dn;      // shifts of the hop terms
   int p2_up, p2_dn;      // log2 |mt| when |mt| is a power of two, else -1
   int sh_d;              // shift of the diagonal term
+  int d_tz;              // >= 0: narrow diagonal (see FxTables::dtz), -1: 128-bit products
   const int64_t* yin;    // accumulated input (may alias y) or null
   int64_t m_in;
   int sh_in;

@@ -131,6 +131,7 @@ struct FxTables {
   DevBuf<int64_t> dup, ddn, wdn;  // diagonal in units of 2^-G
   int64_t U = 0;
   int G = 0;
+  int dtz = -1;  // >= 0: every diagonal entry is a multiple of 2^dtz with |D| >> dtz < 2^6
   double bound = 0.0;  // bound on |H|_inf
   int b = 0;
   uint32_t band = 0;  // rows per band of the down-spin pass

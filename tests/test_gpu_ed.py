@@ -191,17 +191,20 @@ def test_fixed_point_product_matches_reference(pg, tag):
     assert np.max(np.abs(y2 - 0.25 - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
+@pytest.mark.parametrize("mu", [4.0, 3.7])
 @pytest.mark.parametrize("slabs", ["1", "2"])
 @pytest.mark.parametrize("shape,n", [((4, 3), 12), ((13, 1), 10)])
-def test_fixed_point_product_slab_variants(pg, monkeypatch, slabs, shape, n):
+def test_fixed_point_product_slab_variants(pg, monkeypatch, slabs, shape, n, mu):
     """Pass U with one and two slabs per round, on an even half basis (4x3,
     du = 924: 16-byte pass D loads) and an odd one (13-site chain, 5+5
     electrons, du = 1287: split bulk copies, 8-byte pass D loads), against
-    the oracle on the same seeded vector."""
+    the oracle on the same seeded vector.  mu = 4 gives small-integer
+    diagonal energies (one 64-bit product per diagonal term), mu = 3.7 does
+    not (128-bit products)."""
     import models
     monkeypatch.setenv("QCMG_FX_SLABS", slabs)
     ns, nb, ops = models.hubbard_cluster(*shape)
-    params = {"t": 1.0, "U": 8.0, "mu": 4.0}
+    params = {"t": 1.0, "U": 8.0, "mu": mu}
     m = pg.ClusterModel(ns, nb)
     for name, (typ, els) in ops.items():
         if name in params:
