@@ -309,6 +309,18 @@ bool fx_prepare(qcmg_hamiltonian* H) {
     if (H->inter_kind == QCMG_INTER_ONSITE) fold(H->U);
     const double dbound = std::ceil(dmax * scale);
     T.dtz = (std::ldexp(dbound, -tz) < 64.0) ? tz : -1;
+    if (T.dtz >= 0) {
+      auto narrow = [&](const std::vector<double>& src, DevBuf<int32_t>& dst) {
+        std::vector<int32_t> h(std::max<size_t>(src.size(), 1), 0);
+        for (size_t k = 0; k < src.size(); ++k) h[k] = (int32_t)(std::llrint(src[k] * scale) >> T.dtz);
+        dst.upload(h.data(), h.size(), s);
+      };
+      narrow(hdu, T.dup32);
+      narrow(hdd, T.ddn32);
+      narrow(hw, T.wdn32);
+      T.U32 = (int32_t)(std::llrint(H->U * scale) >> T.dtz);
+      QCMG_CUDA(cudaStreamSynchronize(s));  // host staging vectors go out of scope
+    }
   }
   T.bound = dmax + T.t_up * T.maxdeg_up + T.t_dn * T.maxdeg_dn;
   T.b = ceil_log2(std::max(T.bound, 1.0));
@@ -423,6 +435,22 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
     A.sh_in = Eo - yin->E - e;
     A.p2_in = pow2_exponent(A.m_in);
   }
+  // fixed shifts of the FAST kernels (used only when every multiplier is a
+  // power of two and the diagonal is narrow)
+  auto fixed = [](int t, int* to, int64_t* ro) {
+    t = std::min(t, 63);
+    *to = t;
+    *ro = t > 0 ? (int64_t)(1ull << (t - 1)) : 0;
+  };
+  fixed(A.sh_up - A.p2_up, &A.t_up, &A.r_up);
+  fixed(A.sh_dn - A.p2_dn, &A.t_dn, &A.r_dn);
+  fixed(A.sh_d - T.dtz, &A.t_d, &A.r_d);
+  fixed(A.sh_in - A.p2_in, &A.t_in, &A.r_in);
+  A.neg_in = A.m_in < 0;
+  A.dup32 = T.dup32.p;
+  A.ddn32 = T.ddn32.p;
+  A.wdn32 = T.wdn32.p;
+  A.U32 = T.U32;
   A.x = x.buf.p;
   A.y = y.buf.p;
   A.band = T.band;

@@ -74,9 +74,31 @@ __device__ __forceinline__ int64_t round_shift(int64_t v, int t) {
   return (v + (1ll << (t - 1))) >> t;
 }
 
+// round_shift with the shift t and the round term r = 2^(t-1) fixed for a
+// launch (t <= 0: v * 2^-t).  The host clamps t to 63, where |v| < 2^62
+// gives 0 as round_shift does.
+__device__ __forceinline__ int64_t rshift_fixed(int64_t v, int t, int64_t r) {
+  return t > 0 ? (v + r) >> t : (int64_t)((uint64_t)v << (-t));
+}
+
 __device__ __forceinline__ int64_t mul_fix_p2(int64_t a, int64_t m, int s, int p) {
   if (p >= 0) return round_shift(m < 0 ? -a : a, s - p);
   return mul_fix(a, m, s);
+}
+
+// Compile-time forms for kernels specialized on the multipliers: FAST = the
+// multiplier is +-2^p and the diagonal is narrow, so no 128-bit code is
+// generated at all (a runtime test alone leaves both forms in the kernel).
+template <bool FAST>
+__device__ __forceinline__ int64_t scale_term(int64_t a, int64_t m, int s, int p) {
+  if (FAST) return round_shift(m < 0 ? -a : a, s - p);
+  return mul_fix(a, m, s);
+}
+
+template <bool FAST>
+__device__ __forceinline__ int64_t diag_term(int64_t x, int64_t D, int s, int tz) {
+  if (FAST) return round_shift(x * (D >> tz), s - tz);
+  return mul_fix(x, D, s);
 }
 
 // The diagonal term round(x * D / 2^s).  tz >= 0 means D is a multiple of

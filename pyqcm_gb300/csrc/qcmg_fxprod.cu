@@ -18,6 +18,7 @@
 // are a signed sum of gathered entries times t.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 #include <vector>
 
 #include "qcmg_fx.cuh"
@@ -120,7 +121,7 @@ __device__ __forceinline__ void gather_group(uint32_t vbase, uint2 w, int64_t (&
 // columns point at the zero slot du.  With NS = 2 the grid is even, so the
 // two slabs of a round have the same alignment (view offset).  With NS = 1
 // a second CTA on the SM computes while this one's copy is in flight.
-template <int INTER, int NS>
+template <int INTER, int NS, bool FAST>
 __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_passU4(FxProdArgs A) {
   extern __shared__ __align__(16) int64_t smem_slab[];
   __shared__ __align__(8) uint64_t bars[NS];
@@ -173,11 +174,15 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
     slab_range(a0, du, &e0, &e1);
     const int64_t* view = smem_slab + e0;
     int64_t dda[NS];
+    int32_t dda32[NS];
     uint32_t dbits[NS];
+    bool live[NS];
 #pragma unroll
     for (int s = 0; s < NS; ++s) {
       const uint32_t a = min(a0 + s * G, dd - 1u);
-      dda[s] = A.ddn[a];
+      live[s] = a0 + s * G < dd;
+      dda[s] = FAST ? 0 : A.ddn[a];
+      dda32[s] = FAST ? A.ddn32[a] : 0;
       dbits[s] = A.bin_dn[a];
       if (tid == 0 && a0 + s * G < dd) {
         int64_t* v = smem_slab + s * kSlab1Off + e0;
@@ -202,12 +207,13 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
       uint2 w[kPreGroups];
 #pragma unroll
       for (int g = 0; g < kPreGroups; ++g) w[g] = __ldg(A.ell4 + (size_t)g * du + i);
-      const int64_t dui = __ldg(A.dup + i);
+      const int64_t dui = FAST ? 0 : __ldg(A.dup + i);
+      const int32_t dui32 = FAST ? __ldg(A.dup32 + i) : 0;
       const uint32_t ubits = __ldg(A.bin_up + i);
       int64_t yv[NS];
 #pragma unroll
       for (int s = 0; s < NS; ++s)
-        yv[s] = (A.yin && a0 + s * G < dd) ? __ldcs(A.yin + (size_t)(a0 + s * G) * du + i) : 0;
+        yv[s] = (A.yin && live[s]) ? __ldcs(A.yin + (size_t)(a0 + s * G) * du + i) : 0;
       if (i + bd < du) c_next = __ldg(A.cnt4 + i + bd);
       int64_t sp[NS], sn[NS];
 #pragma unroll
@@ -237,24 +243,42 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
       }
 #pragma unroll
       for (int s = 0; s < NS; ++s) {
+        if (!live[s]) break;
         const uint32_t a = a0 + s * G;
-        if (a >= dd) break;
-        const size_t base = (size_t)a * du;
-        int64_t out = mul_fix_p2(sp[s] - sn[s], A.mt_up, A.sh_up, A.p2_up);
-        int64_t D = dui + dda[s];
-        if (INTER == QCMG_INTER_ONSITE) {
-          D += A.U * (int64_t)__popc(ubits & dbits[s]);
-        } else if (INTER == QCMG_INTER_GENERAL) {
-          uint32_t u = ubits;
-          const int64_t* wt = A.wdn + (size_t)a * A.L;
-          while (u) {
-            D += wt[__ffs(u) - 1];
-            u &= u - 1;
+        int64_t out;
+        if (FAST) {
+          // small-integer diagonal D >> tz in 32 bits, shifts fixed per launch
+          out = rshift_fixed(sp[s] - sn[s], A.t_up, A.r_up);
+          int32_t Dn = dui32 + dda32[s];
+          if (INTER == QCMG_INTER_ONSITE) {
+            Dn += A.U32 * __popc(ubits & dbits[s]);
+          } else if (INTER == QCMG_INTER_GENERAL) {
+            uint32_t u = ubits;
+            const int32_t* wt = A.wdn32 + (size_t)a * A.L;
+            while (u) {
+              Dn += wt[__ffs(u) - 1];
+              u &= u - 1;
+            }
           }
+          out += rshift_fixed(view[s * kSlab1Off + i] * (int64_t)Dn, A.t_d, A.r_d);
+          if (A.yin) out += rshift_fixed(A.neg_in ? -yv[s] : yv[s], A.t_in, A.r_in);
+        } else {
+          out = mul_fix(sp[s] - sn[s], A.mt_up, A.sh_up);
+          int64_t D = dui + dda[s];
+          if (INTER == QCMG_INTER_ONSITE) {
+            D += A.U * (int64_t)__popc(ubits & dbits[s]);
+          } else if (INTER == QCMG_INTER_GENERAL) {
+            uint32_t u = ubits;
+            const int64_t* wt = A.wdn + (size_t)a * A.L;
+            while (u) {
+              D += wt[__ffs(u) - 1];
+              u &= u - 1;
+            }
+          }
+          out += mul_fix(view[s * kSlab1Off + i], D, A.sh_d);
+          if (A.yin) out += mul_fix(yv[s], A.m_in, A.sh_in);
         }
-        out += mul_fix_diag(view[s * kSlab1Off + i], D, A.sh_d, A.d_tz);
-        if (A.yin) out += mul_fix_p2(yv[s], A.m_in, A.sh_in, A.p2_in);
-        __stcs(A.y + base + i, out);
+        __stcs(A.y + (size_t)a * du + i, out);
       }
     }
     __syncthreads();  // every buffer is free again
@@ -295,7 +319,7 @@ __device__ __forceinline__ void passD_accum(const int64_t* __restrict__ x, uint3
 
 // VEC = 2 needs du even (every slab segment at an even row is 16-byte
 // aligned); bands start at multiples of 256 rows.
-template <int VEC>
+template <int VEC, bool FAST>
 __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
   const uint32_t du = A.du, dd = A.dd;
   const uint32_t lane = threadIdx.x & 31u;
@@ -322,26 +346,27 @@ __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
         passD_accum<VEC>(A.x, du, ccol, spos, e, ia, ib, va, vb, N);
       }
       // y streams through once (evict-first), leaving L2 to the band of x
-      const int64_t m = A.mt_dn;
-      const int sh = A.sh_dn, p2 = A.p2_dn;
+      auto term = [&](int64_t v) {
+        return FAST ? rshift_fixed(v, A.t_dn, A.r_dn) : mul_fix(v, A.mt_dn, A.sh_dn);
+      };
       if (VEC == 2) {
         if (va) {
           longlong2* yp = reinterpret_cast<longlong2*>(yrow + ia);
           longlong2 v = __ldcs(yp);
-          v.x += mul_fix_p2(P[0] - N[0], m, sh, p2);
-          v.y += mul_fix_p2(P[1] - N[1], m, sh, p2);
+          v.x += term(P[0] - N[0]);
+          v.y += term(P[1] - N[1]);
           __stcs(yp, v);
         }
         if (vb) {
           longlong2* yp = reinterpret_cast<longlong2*>(yrow + ib);
           longlong2 v = __ldcs(yp);
-          v.x += mul_fix_p2(P[2] - N[2], m, sh, p2);
-          v.y += mul_fix_p2(P[3] - N[3], m, sh, p2);
+          v.x += term(P[2] - N[2]);
+          v.y += term(P[3] - N[3]);
           __stcs(yp, v);
         }
       } else {
-        if (va) __stcs(yrow + ia, __ldcs(yrow + ia) + mul_fix_p2(P[0] - N[0], m, sh, p2));
-        if (vb) __stcs(yrow + ib, __ldcs(yrow + ib) + mul_fix_p2(P[1] - N[1], m, sh, p2));
+        if (va) __stcs(yrow + ia, __ldcs(yrow + ia) + term(P[0] - N[0]));
+        if (vb) __stcs(yrow + ib, __ldcs(yrow + ib) + term(P[1] - N[1]));
       }
     }
   }
@@ -451,15 +476,28 @@ void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t
   int sms = 0;
   QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
   const int ik = H->inter_kind;
+  // FAST kernels: hop magnitudes and accumulation factor are powers of two
+  // and the diagonal is narrow (the Hubbard form with t = 1 and small-integer
+  // energies); everything else uses the 128-bit products
+  const bool fast = A.d_tz >= 0 && A.p2_up >= 0 && A.p2_dn >= 0 && (!A.yin || A.p2_in >= 0);
+  auto passU4 = [&](auto ns_tag, auto fast_tag) {
+    constexpr int NS = decltype(ns_tag)::value;
+    constexpr bool F = decltype(fast_tag)::value;
+    if (ik == QCMG_INTER_NONE) launch_passU4<NS>(k_fx_passU4<QCMG_INTER_NONE, NS, F>, H, A, sms, s);
+    else if (ik == QCMG_INTER_ONSITE) launch_passU4<NS>(k_fx_passU4<QCMG_INTER_ONSITE, NS, F>, H, A, sms, s);
+    else launch_passU4<NS>(k_fx_passU4<QCMG_INTER_GENERAL, NS, F>, H, A, sms, s);
+  };
+  using One = std::integral_constant<int, 1>;
+  using Two = std::integral_constant<int, 2>;
+  using Fast = std::true_type;
+  using Full = std::false_type;
   // pass U
   if (T.ns == 2) {
-    if (ik == QCMG_INTER_NONE) launch_passU4<2>(k_fx_passU4<QCMG_INTER_NONE, 2>, H, A, sms, s);
-    else if (ik == QCMG_INTER_ONSITE) launch_passU4<2>(k_fx_passU4<QCMG_INTER_ONSITE, 2>, H, A, sms, s);
-    else launch_passU4<2>(k_fx_passU4<QCMG_INTER_GENERAL, 2>, H, A, sms, s);
+    if (fast) passU4(Two{}, Fast{});
+    else passU4(Two{}, Full{});
   } else if (T.ns == 1) {
-    if (ik == QCMG_INTER_NONE) launch_passU4<1>(k_fx_passU4<QCMG_INTER_NONE, 1>, H, A, sms, s);
-    else if (ik == QCMG_INTER_ONSITE) launch_passU4<1>(k_fx_passU4<QCMG_INTER_ONSITE, 1>, H, A, sms, s);
-    else launch_passU4<1>(k_fx_passU4<QCMG_INTER_GENERAL, 1>, H, A, sms, s);
+    if (fast) passU4(One{}, Fast{});
+    else passU4(One{}, Full{});
   } else {
     const size_t smem = (size_t)H->du * 8;
     const int threads = H->du >= 512 ? 512 : (H->du >= 256 ? 256 : 128);
@@ -477,10 +515,13 @@ void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t
   // pass D
   const size_t items = (size_t)A.nbands * H->dd;
   const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * 8));
-  if ((H->du & 1u) == 0u)
-    k_fx_passD4<2><<<gD, 256, 0, s>>>(A);
-  else
-    k_fx_passD4<1><<<gD, 256, 0, s>>>(A);
+  if ((H->du & 1u) == 0u) {
+    if (fast) k_fx_passD4<2, true><<<gD, 256, 0, s>>>(A);
+    else k_fx_passD4<2, false><<<gD, 256, 0, s>>>(A);
+  } else {
+    if (fast) k_fx_passD4<1, true><<<gD, 256, 0, s>>>(A);
+    else k_fx_passD4<1, false><<<gD, 256, 0, s>>>(A);
+  }
   QCMG_CUDA(cudaGetLastError());
 }
 

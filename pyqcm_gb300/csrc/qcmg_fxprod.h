@@ -38,6 +38,16 @@ struct FxProdArgs {
   int64_t* y;
   uint32_t band;  // rows per band (pass D)
   uint32_t nbands;
+  // FAST kernels (powers-of-two multipliers, narrow diagonal): the diagonal
+  // tables shifted right by d_tz as int32, and each term's shift t with its
+  // round term r = 2^(t-1) (rshift_fixed)
+  const int32_t* dup32;
+  const int32_t* ddn32;
+  const int32_t* wdn32;
+  int32_t U32;
+  int t_up, t_dn, t_d, t_in;
+  int64_t r_up, r_dn, r_d, r_in;
+  int neg_in;  // the accumulation factor is negative
   // grouped ELL form of the up half-operator (see build_ell4)
   const uint2* ell4;
   const uint16_t* cnt4;

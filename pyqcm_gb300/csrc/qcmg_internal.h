@@ -132,6 +132,8 @@ struct FxTables {
   int64_t U = 0;
   int G = 0;
   int dtz = -1;  // >= 0: every diagonal entry is a multiple of 2^dtz with |D| >> dtz < 2^6
+  DevBuf<int32_t> dup32, ddn32, wdn32;  // the diagonal tables >> dtz (when dtz >= 0)
+  int32_t U32 = 0;
   double bound = 0.0;  // bound on |H|_inf
   int b = 0;
   uint32_t band = 0;  // rows per band of the down-spin pass
