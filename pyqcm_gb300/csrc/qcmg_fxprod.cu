@@ -401,21 +401,69 @@ bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const De
   groups = std::max<uint32_t>(groups, kPreGroups);  // pass U loads the first kPreGroups unconditionally
   const uint16_t Z = (uint16_t)dim;
   std::vector<uint16_t> cols((size_t)groups * 4 * dim, Z), hc(dim);
-  // cols is laid out as [group][row][4]; each sign list is sorted, so the
-  // k-th columns of neighbouring rows tend to be close (fewer shared-memory
-  // bank conflicts between the lanes of a warp)
-  std::vector<uint32_t> tmp;
+  // cols is laid out as [group][row][4].  Slot k of a row (group k/4,
+  // position k%4) is gathered by 16 lanes at once: the rows of one
+  // half-warp, 16 consecutive rows from a multiple of 16.  An 8-byte shared
+  // load costs one wavefront per distinct address on its busiest bank pair
+  // (column mod 16), and a row's columns may take any order within its
+  // positive and its negative list.  So, slot by slot, each row of a
+  // half-warp takes the remaining column of the slot's sign list whose bank
+  // pair is least used so far in that slot; rows with the fewest choices go
+  // first.  On the 4x4 half bases this cuts the wavefronts from ~1.8x to
+  // ~1.55x the conflict-free count.
   for (uint32_t i = 0; i < dim; ++i) {
     const uint32_t np = hrs[i] - hrp[i], nn = hrp[i + 1] - hrs[i];
-    const uint32_t gp = (np + 3) / 4, gn = (nn + 3) / 4;
-    tmp.assign(hcol.begin() + hrp[i], hcol.begin() + hrs[i]);
-    std::sort(tmp.begin(), tmp.end());
-    for (uint32_t k = 0; k < np; ++k) cols[((size_t)(k / 4) * dim + i) * 4 + (k % 4)] = (uint16_t)tmp[k];
-    tmp.assign(hcol.begin() + hrs[i], hcol.begin() + hrp[i + 1]);
-    std::sort(tmp.begin(), tmp.end());
-    for (uint32_t k = 0; k < nn; ++k)
-      cols[((size_t)(gp + k / 4) * dim + i) * 4 + (k % 4)] = (uint16_t)tmp[k];
-    hc[i] = (uint16_t)(gp | (gn << 8));
+    hc[i] = (uint16_t)(((np + 3) / 4) | (((nn + 3) / 4) << 8));
+  }
+  std::vector<std::vector<uint32_t>> remp(16), remn(16);
+  std::vector<uint32_t> order;
+  for (uint32_t b0 = 0; b0 < dim; b0 += 16) {
+    const uint32_t nr = std::min<uint32_t>(16, dim - b0);
+    uint32_t kmax = 0;
+    for (uint32_t r = 0; r < nr; ++r) {
+      const uint32_t i = b0 + r;
+      remp[r].assign(hcol.begin() + hrp[i], hcol.begin() + hrs[i]);
+      remn[r].assign(hcol.begin() + hrs[i], hcol.begin() + hrp[i + 1]);
+      std::sort(remp[r].begin(), remp[r].end());
+      std::sort(remn[r].begin(), remn[r].end());
+      kmax = std::max<uint32_t>(kmax, 4u * ((hc[i] & 0xffu) + (hc[i] >> 8)));
+    }
+    for (uint32_t k = 0; k < kmax; ++k) {
+      // the list slot k draws from, for row r (null: padding)
+      auto list = [&](uint32_t r) -> std::vector<uint32_t>* {
+        const uint32_t c = hc[b0 + r], gp = c & 0xffu, gt = gp + (c >> 8);
+        if (k < 4 * gp) return &remp[r];
+        if (k < 4 * gt) return &remn[r];
+        return nullptr;
+      };
+      order.resize(nr);
+      for (uint32_t r = 0; r < nr; ++r) order[r] = r;
+      std::stable_sort(order.begin(), order.end(), [&](uint32_t p, uint32_t q) {
+        const std::vector<uint32_t>* lp = list(p);
+        const std::vector<uint32_t>* lq = list(q);
+        const size_t np = (lp && !lp->empty()) ? lp->size() : SIZE_MAX;
+        const size_t nq = (lq && !lq->empty()) ? lq->size() : SIZE_MAX;
+        return np < nq;
+      });
+      uint32_t used[16] = {0};
+      bool zero_used = false;
+      for (uint32_t r : order) {
+        std::vector<uint32_t>* l = list(r);
+        uint32_t j = Z;
+        if (l && !l->empty()) {
+          size_t best = 0;
+          for (size_t q = 1; q < l->size(); ++q)
+            if (used[(*l)[q] % 16] < used[(*l)[best] % 16]) best = q;
+          j = (*l)[best];
+          l->erase(l->begin() + best);
+          ++used[j % 16];
+        } else if (!zero_used) {  // padding: every padded lane reads the same zero slot
+          zero_used = true;
+          ++used[Z % 16];
+        }
+        cols[((size_t)(k / 4) * dim + b0 + r) * 4 + (k % 4)] = (uint16_t)j;
+      }
+    }
   }
   std::vector<uint2> he((size_t)groups * dim);
   for (size_t q = 0; q < he.size(); ++q) {
