@@ -294,6 +294,130 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def _fp64_peak():
+    """FP64 FMA rate of the device in TFLOP/s (measured on the GB300s
+    with a probe kernel; MEASURED_PEAKS.json carries no FP64 figure)."""
+    return 1.0
+
+
+def run_lanczos(args):
+    """4x4 N=16 Lanczos ground state to 1e-10 (the reference's recurrence,
+    no reorthogonalization), energy only: time to solution and the per-
+    iteration bytes (product 24 D + fused update/norm 16 D)."""
+    import torch
+    import pyqcm_gb300 as pg
+    torch.cuda.set_device(0)
+    ns, nb, ops = model_ops()
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, PARAMS, sector_of(NX, NY)[0])
+    D = H.dim
+    e0, _, alpha, _ = H.lanczos(tol=1e-10, max_iter=600, want_psi=False)  # warm-up run
+    t0 = time.perf_counter()
+    e0, _, alpha, _ = H.lanczos(tol=1e-10, max_iter=600, want_psi=False)
+    dt = time.perf_counter() - t0
+    nit = len(alpha)
+    per_iter = dt / nit
+    gbs = 40.0 * D / per_iter / 1e9
+    peak, kind = measured_peak()
+    print(json.dumps({"metric": "lanczos_ground_state_s", "value": dt, "unit": "s",
+                      "higher_is_better": False, "iterations": nit, "E0": e0,
+                      "ms_per_iteration": per_iter * 1e3,
+                      "bytes_per_iteration": 40 * D, "gbs_per_iteration": gbs,
+                      "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s",
+                                   "frac": gbs / peak, "peak_kind": kind},
+                      "dtype": "int64", "data": "synthetic",
+                      "config": {"workload": f"{NX}x{NY} Hubbard cluster, t=1 U=8 mu=4, sector "
+                                             f"{sector_of(NX, NY)[0]} (dim {D:,}), Lanczos to 1e-10",
+                                 "dim": D}}))
+
+
+def _vca_3x4():
+    """3x4 cluster, t=1 t'=-0.3 U=8 mu=4, AF Weiss field M (configs' VCA case)."""
+    import pyqcm_gb300 as pg
+    from pyqcm_gb300.lattice import LatticeModel
+    cm = pg.ClusterModel(12, 0)
+    sites = [(x, y, 0) for y in range(3) for x in range(4)]
+    lm = LatticeModel(cm, sites, [(4, 0, 0), (0, 3, 0)])
+    lm.interaction_operator("U", 1.0)
+    lm.hopping_operator("t", (1, 0, 0), -1.0)
+    lm.hopping_operator("t", (0, 1, 0), -1.0)
+    lm.hopping_operator("tp", (1, 1, 0), -1.0)
+    lm.hopping_operator("tp", (-1, 1, 0), -1.0)
+    lm.density_wave("M", "Z", (1, 1, 0), 1.0, 0.0)
+    lm.set_target_sectors("R0:N12:S0")
+    lm.set_parameters({"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0, "M": 0.0, "M_1": 0.1})
+    return lm
+
+
+def run_sef(args):
+    """VCA Potthoff functional on the 128x128 k grid x 256 Gauss-Legendre
+    frequencies (2 spins, 12x12 blocks): the cluster solve (ground state +
+    Green function, FP64 product since t' != t) and the grid integral."""
+    import torch
+    from pyqcm_gb300 import _lib, lattice as lat
+    torch.cuda.set_device(0)
+    lat.set_wavevector_grid(128, 128, 1)
+    w, wt = lat.legendre_frequency_grid(1.0, 10.0, 64, 128, 64)
+    lat.discrete_integration_grid(w, wt)
+    lm = _vca_3x4()
+    inst = lm.instance()
+    t0 = time.perf_counter()
+    omega = inst.Potthoff_functional()
+    t_total = time.perf_counter() - t0
+    blocks = inst._spin_blocks()
+    t1 = time.perf_counter()
+    for blk in blocks.values():
+        out = _lib.c_double()
+        _lib.check(_lib.lib().qcmg_sef_grid(blk._h, len(w), _lib.ptr(w), _lib.ptr(wt), 128, 128, 1,
+                                            out))
+    t_grid = time.perf_counter() - t1
+    L = 12
+    points = 128 * 128 * len(w) * len(blocks)
+    flops = points * (8 * L ** 3 + 8 * L ** 3 / 3)  # per-point count of the reference's integrand
+    print(json.dumps({"metric": "vca_sef_s_per_M_value", "value": t_total, "unit": "s",
+                      "higher_is_better": False, "omega": omega, "sef_grid_s": t_grid,
+                      "points": points, "points_per_s": points / t_grid,
+                      "alg_tflops": flops / t_grid / 1e12,
+                      "fp64_peak_tflops": _fp64_peak(),
+                      "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "3x4 cluster t=1 t'=-0.3 U=8 mu=4 M_1=0.1, sector "
+                                             "R0:N12:S0, 128x128 k x 256 frequencies, 2 spins"}}))
+
+
+def run_cpt(args):
+    """CPT spectral function of the 8-site chain: 256 k x 512 real
+    frequencies in [-8, 8], eta = 0.1."""
+    import numpy as np
+    import torch
+    import pyqcm_gb300 as pg
+    from pyqcm_gb300.lattice import LatticeModel
+    torch.cuda.set_device(0)
+    cm = pg.ClusterModel(8, 0)
+    lm = LatticeModel(cm, [(i, 0, 0) for i in range(8)], [(8, 0, 0)])
+    lm.interaction_operator("U", 1.0)
+    lm.hopping_operator("t", (1, 0, 0), -1.0)
+    lm.set_target_sectors("R0:N8:S0")
+    lm.set_parameters({"t": 1.0, "U": 4.0, "mu": 2.0})
+    inst = lm.instance()
+    k = np.zeros((256, 3))
+    k[:, 0] = np.arange(256) / 256.0
+    w = np.linspace(-8.0, 8.0, 512)
+    t0 = time.perf_counter()
+    A = inst.spectral_function(w, k, eta=0.1)  # includes the cluster solve
+    t_first = time.perf_counter() - t0
+    t1 = time.perf_counter()
+    A = inst.spectral_function(w, k, eta=0.1)
+    t_map = time.perf_counter() - t1
+    print(json.dumps({"metric": "cpt_spectral_map_s", "value": t_map, "unit": "s",
+                      "higher_is_better": False, "with_cluster_solve_s": t_first,
+                      "points": int(A.size), "points_per_s": A.size / t_map,
+                      "dtype": "f64", "data": "synthetic",
+                      "config": {"workload": "8-site chain t=1 U=4 mu=2, 256 k x 512 w in [-8,8], "
+                                             "eta=0.1"}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,12 +429,20 @@ def main():
                     help="NXxNY Hubbard cluster at half filling (profiling of smaller cases)")
     ap.add_argument("--electrons", type=int, default=None,
                     help="electrons in the sector (default: half filling)")
+    ap.add_argument("--workload", default="product", choices=["product", "lanczos", "sef", "cpt"],
+                    help="product (the headline line) or one of the secondary measurements")
     args = ap.parse_args()
     global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))
     NEL = args.electrons
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "lanczos":
+        run_lanczos(args)
+    elif args.workload == "sef":
+        run_sef(args)
+    elif args.workload == "cpt":
+        run_cpt(args)
     else:
         run_gpu(args)
 

@@ -138,21 +138,34 @@ __device__ __forceinline__ void block_store128(I128 s, I128* part) {
   }
 }
 
+// Exact <a, b> partials, two elements per 16-byte load (the fixed-point
+// vectors come from cudaMalloc, so even indices are 16-byte aligned); the
+// integer sums are exact, so the summation order does not matter.
 __global__ void __launch_bounds__(256) k_fx_dot(const int64_t* __restrict__ a,
                                                 const int64_t* __restrict__ b, size_t n,
                                                 I128* __restrict__ part) {
   I128 s = {0, 0};
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x)
-    s = add128(s, shr128(mul_s64(a[i], b[i]), kDotShift));
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t n2 = n / 2;
+  const longlong2* a2 = reinterpret_cast<const longlong2*>(a);
+  const longlong2* b2 = reinterpret_cast<const longlong2*>(b);
+#pragma unroll 2
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n2; j += stride) {
+    const longlong2 x = __ldcs(a2 + j), y = __ldcs(b2 + j);
+    s = add128(s, shr128(mul_s64(x.x, y.x), kDotShift));
+    s = add128(s, shr128(mul_s64(x.y, y.y), kDotShift));
+  }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+    s = add128(s, shr128(mul_s64(a[n - 1], b[n - 1]), kDotShift));
   block_store128(s, part);
 }
 
+// Sum of the block partials by one warp (launched with 32 threads).
 __global__ void k_fx_final(const I128* __restrict__ part, int np, I128* __restrict__ out) {
-  if (threadIdx.x != 0) return;
   I128 s = {0, 0};
-  for (int i = 0; i < np; ++i) s = add128(s, part[i]);
-  *out = s;
+  for (int i = threadIdx.x; i < np; i += blockDim.x) s = add128(s, part[i]);
+  s = warp_sum128(s);
+  if (threadIdx.x == 0) *out = s;
 }
 
 // Fused Lanczos update:
@@ -166,15 +179,32 @@ __global__ void __launch_bounds__(256) k_fx_update(int64_t* __restrict__ w,
                                                    unsigned long long* __restrict__ qmax) {
   I128 s = {0, 0};
   unsigned long long m = 0;
-  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
-       i += (size_t)gridDim.x * blockDim.x) {
-    int64_t o = shr_round(w[i], sw);
-    if (ma) o -= mul_fix(v[i], ma, sa);
-    if (p && mb) o -= mul_fix(p[i], mb, sb);
-    w[i] = o;
+  auto one = [&](int64_t wi, int64_t vi, int64_t pi) {
+    int64_t o = shr_round(wi, sw);
+    if (ma) o -= mul_fix(vi, ma, sa);
+    if (p && mb) o -= mul_fix(pi, mb, sb);
     s = add128(s, shr128(mul_s64(o, o), kDotShift));
     m = max(m, (unsigned long long)(o < 0 ? -o : o));
+    return o;
+  };
+  // two elements per 16-byte load (cudaMalloc'd vectors: even indices are
+  // 16-byte aligned); w, v and p are each read once and streamed
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const size_t n2 = n / 2;
+  longlong2* w2 = reinterpret_cast<longlong2*>(w);
+  const longlong2* v2 = reinterpret_cast<const longlong2*>(v);
+  const longlong2* p2 = reinterpret_cast<const longlong2*>(p);
+#pragma unroll 2
+  for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n2; j += stride) {
+    const longlong2 wv = __ldcs(w2 + j), vv = __ldcs(v2 + j);
+    const longlong2 pv = p ? __ldcs(p2 + j) : make_longlong2(0, 0);
+    longlong2 o;
+    o.x = one(wv.x, vv.x, pv.x);
+    o.y = one(wv.y, vv.y, pv.y);
+    __stcs(w2 + j, o);
   }
+  if ((n & 1) && blockIdx.x == 0 && threadIdx.x == 0)
+    w[n - 1] = one(w[n - 1], v[n - 1], p ? p[n - 1] : 0);
   for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
   if ((threadIdx.x & 31) == 0) atomicMax(qmax, m);
   block_store128(s, part);
@@ -589,8 +619,13 @@ LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, 
           throw Error(QCMG_ERR_NOCONV,
                       "Lanczos procedure exceeded " + std::to_string(max_iter) + " iterations");
       }
-      // rotate: p <- v, v <- w / beta, w <- old p
-      w->c = w->c / b;
+      // rotate: p <- v, v <- w / beta, w <- old p.  The division only changes
+      // the lazy scale; its power of two moves into the exponent (exact), so
+      // c stays in [0.5, 1) and neither c nor 2^E drifts out of double range
+      // over hundreds of iterations.
+      int k2 = 0;
+      w->c = std::frexp(w->c / b, &k2);
+      w->E += k2;
       FxVec* t = p;
       p = v;
       v = w;

@@ -160,6 +160,10 @@ struct qcmg_hamiltonian {
   cudaStream_t own_stream = nullptr;  // created with the handle
   // staging for host-pointer calls
   qcmg::DevBuf<double> xbuf, ybuf;
+  // the seeded Lanczos start vector of the last seed used (generated once)
+  qcmg::DevBuf<double> seed_vec;
+  unsigned seed_key = 0;
+  bool seed_ok = false;
   // deterministic reduction scratch
   qcmg::DevBuf<double> partials;
   qcmg::DevBuf<double> scalars;

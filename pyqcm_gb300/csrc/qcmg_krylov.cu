@@ -159,24 +159,39 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
   cudaStream_t s = H->stream;
   LanczosResult res;
   QCMG_CHECK_ARG(n > 0, "empty sector");
-  std::vector<double> hx0;
+  // Start vector: the caller's, or the seeded one.  The seeded vector is
+  // generated on the host (the reference's sequential std::normal_distribution
+  // stream, bit for bit) and kept on the device per handle, so repeated solves
+  // of a sector (VCA / CDMFT loops) generate it once.
+  DevVec x0_own(x0_host ? n : 1);
+  const double* x0_dev = nullptr;
   if (!x0_host) {
-    hx0.resize(n);
-    seeded_vector(n, seed, hx0.data());
-    x0_host = hx0.data();
+    if (!(H->seed_ok && H->seed_key == seed && H->seed_vec.n == n)) {
+      H->seed_ok = false;
+      std::vector<double> hx0(n);
+      seeded_vector(n, seed, hx0.data());
+      H->seed_vec.upload(hx0.data(), n, s);
+      QCMG_CUDA(cudaStreamSynchronize(s));  // hx0 goes out of scope
+      H->seed_key = seed;
+      H->seed_ok = true;
+    }
+    x0_dev = H->seed_vec.p;
+  } else {
+    QCMG_CUDA(cudaMemcpyAsync(x0_own.p, x0_host, n * 8, cudaMemcpyHostToDevice, s));
+    x0_dev = x0_own.p;
   }
-  DevVec x0(n), r(n), q(n);
-  QCMG_CUDA(cudaMemcpyAsync(x0.p, x0_host, n * 8, cudaMemcpyHostToDevice, s));
   if (reorth <= 0 && H->use_fx && fx_prepare(H)) {
     // fixed-point fast path (one hop magnitude per spin)
-    LanczosResult fr = fx_lanczos(H, x0.p, tol, max_iter, psi_host ? r.p : nullptr);
+    DevVec psi_dev(psi_host ? n : 1);
+    LanczosResult fr = fx_lanczos(H, x0_dev, tol, max_iter, psi_host ? psi_dev.p : nullptr);
     if (psi_host) {
-      QCMG_CUDA(cudaMemcpyAsync(psi_host, r.p, n * 8, cudaMemcpyDeviceToHost, s));
+      QCMG_CUDA(cudaMemcpyAsync(psi_host, psi_dev.p, n * 8, cudaMemcpyDeviceToHost, s));
       QCMG_CUDA(cudaStreamSynchronize(s));
     }
     return fr;
   }
-  QCMG_CUDA(cudaMemcpyAsync(r.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+  DevVec r(n), q(n);
+  QCMG_CUDA(cudaMemcpyAsync(r.p, x0_dev, n * 8, cudaMemcpyDeviceToDevice, s));
   QCMG_CUDA(cudaMemsetAsync(q.p, 0, n * 8, s));
   Reducer red;
   std::vector<double> z;
@@ -206,9 +221,9 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
     if (psi_host) {
       // Eigenvector replay of LanczosEigenvector (Lanczos.hpp:109-131).
       DevVec gs(n);
-      QCMG_CUDA(cudaMemcpyAsync(gs.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+      QCMG_CUDA(cudaMemcpyAsync(gs.p, x0_dev, n * 8, cudaMemcpyDeviceToDevice, s));
       scale(gs.p, z[0], n, s);
-      QCMG_CUDA(cudaMemcpyAsync(r.p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+      QCMG_CUDA(cudaMemcpyAsync(r.p, x0_dev, n * 8, cudaMemcpyDeviceToDevice, s));
       QCMG_CUDA(cudaMemsetAsync(q.p, 0, n * 8, s));
       for (size_t j = 1; j < z.size(); ++j) {
         matvec(H, r.p, q.p, true);
@@ -227,7 +242,7 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
   MultiOps mops;
   std::vector<double> c;
   V.emplace_back(n);
-  QCMG_CUDA(cudaMemcpyAsync(V[0].p, x0.p, n * 8, cudaMemcpyDeviceToDevice, s));
+  QCMG_CUDA(cudaMemcpyAsync(V[0].p, x0_dev, n * 8, cudaMemcpyDeviceToDevice, s));
   Vp.push_back(V[0].p);
   double* w = r.p;  // residual
   double ritz = 2.0 * tol;

@@ -307,6 +307,36 @@ def test_fixed_point_product_4x4_full_sector(pg):
     torch.cuda.empty_cache()
 
 
+def test_fixed_point_lanczos_long_run_stays_finite(pg):
+    """700 Lanczos steps without convergence (tolerance 1e-300): the lazy
+    vector scale must not drift out of double range; the run ends with
+    NOCONV, not with a numerical breakdown."""
+    m, params, sec = engine_model("chain8")
+    H = pg.Hamiltonian(m, params, sec)
+    assert H.fx_available()
+    with pytest.raises(pg.QcmgError) as ei:
+        H.lanczos(tol=1e-300, max_iter=700, reorth=0, want_psi=False)
+    assert ei.value.code == -4, ei.value
+
+
+def test_lanczos_4x4_full_sector_both_paths(pg):
+    """4x4 Hubbard cluster, half filling (dim 165,636,900): ground-state
+    energy to 1e-10 on the fixed-point path against the FP64 path (the
+    reference's arithmetic), same seeded start."""
+    _torch()
+    import models
+    ns, nb, ops = models.hubbard_cluster(4, 4)
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, {"t": 1.0, "U": 8.0, "mu": 4.0}, "R0:N16:S0")
+    e_fx, _, a_fx, _ = H.lanczos(tol=1e-10, max_iter=800, reorth=0, want_psi=False)
+    H.set_path(False)
+    e_64, _, a_64, _ = H.lanczos(tol=1e-10, max_iter=800, reorth=0, want_psi=False)
+    assert np.isfinite(e_fx) and np.isfinite(e_64)
+    assert abs(e_fx - e_64) <= 1e-10 * abs(e_64), (e_fx, e_64, len(a_fx), len(a_64))
+
+
 def test_multidot_against_numpy(pg):
     torch = _torch()
     from pyqcm_gb300 import _lib
