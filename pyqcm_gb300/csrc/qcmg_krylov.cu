@@ -73,6 +73,22 @@ __global__ void __launch_bounds__(256) k_multiaxpy(const double* const* __restri
   }
 }
 
+// v <- sc * v, then V_k <- V_k - c_k * v for k < m (the scaled v): one pass
+// over v for the whole Gram-Schmidt sweep of a band-Lanczos step.
+__global__ void __launch_bounds__(256) k_scale_sub(double* __restrict__ v, double sc,
+                                                   double* const* __restrict__ V,
+                                                   const double* __restrict__ c, int m, size_t n) {
+  extern __shared__ double cs[];
+  for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = c[k];
+  __syncthreads();
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double x = v[i] * sc;
+    v[i] = x;
+    for (int k = 0; k < m; ++k) V[k][i] = fma(-cs[k], x, V[k][i]);
+  }
+}
+
 // Block count of a multi-dot over n elements (fixed: deterministic order).
 int multidot_blocks(size_t n) {
   return (int)std::max<size_t>(1, std::min<size_t>((n + kTile - 1) / kTile, 2 * 152));
@@ -122,6 +138,24 @@ struct MultiOps {
     size_t g = std::min<size_t>((n + 255) / 256, 152 * 8);
     k_multiaxpy<<<(unsigned)std::max<size_t>(g, 1), 256, m * sizeof(double), s>>>(ptrs.p, m,
                                                                                    coef.p, w, n);
+    QCMG_CUDA(cudaGetLastError());
+  }
+  // v <- sc v;  V_k <- V_k - c_k v  (k_scale_sub)
+  DevBuf<double*> wptrs;
+  DevBuf<double> wcoef;
+  void scale_sub(double* v, double sc, const std::vector<double*>& V, const std::vector<double>& c,
+                 size_t n, cudaStream_t s) {
+    const int m = (int)V.size();
+    if (n == 0) return;
+    wptrs.alloc(std::max(m, 1));
+    wcoef.alloc(std::max(m, 1));
+    if (m) {
+      QCMG_CUDA(cudaMemcpyAsync(wptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+      QCMG_CUDA(cudaMemcpyAsync(wcoef.p, c.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    size_t g = std::min<size_t>((n + 255) / 256, 152 * 8);
+    k_scale_sub<<<(unsigned)std::max<size_t>(g, 1), 256, std::max(m, 1) * sizeof(double), s>>>(
+        v, sc, wptrs.p, wcoef.p, m, n);
     QCMG_CUDA(cudaGetLastError());
   }
 };
@@ -383,8 +417,22 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   Cusolver solver;
   double ev_old = 1e12;
   int j;
+  std::vector<const double*> tg;
+  std::vector<double*> gs_vecs;
+  std::vector<double> gs_coef;
+  std::vector<const double*> rec_vecs;
+  std::vector<double> rec_coef;
   for (j = 0; j < M0; ++j) {
-    double z = std::sqrt(red.dot(v[j], v[j], n, s));
+    // One multi-dot on the unscaled v_j gives its norm, its projections on
+    // the p start vectors and its dots with the next pc-1 vectors (each of
+    // those vectors is changed only by its own update below, so the dots
+    // are independent): one synchronization instead of pc + 1.
+    tg.clear();
+    tg.push_back(v[j]);
+    for (int k = 0; k < p; ++k) tg.push_back(phip[k]);
+    for (int k = j + 1; k < j + pc; ++k) tg.push_back(v[k]);
+    mops.multidot(tg, v[j], n, s, tmp);
+    double z = std::sqrt(tmp[0]);
     if (z < acc_defl) {
       if (j >= pc) {
         I.push_back(j - pc);
@@ -398,15 +446,19 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
       j--;
       continue;
     }
-    scale(v[j], 1.0 / z, n, s);
+    // v_j /= z; v_k -= <v_j, v_k> v_j for the next pc-1 vectors (one kernel)
+    const double iz = 1.0 / z;
     if (j >= pc) T(j, j - pc) = z;
-    mops.multidot(phip, v[j], n, s, tmp);
-    for (int k = 0; k < p; ++k) P[k + (size_t)p * j] = tmp[k];
+    for (int k = 0; k < p; ++k) P[k + (size_t)p * j] = tmp[1 + k] * iz;
+    gs_vecs.clear();
+    gs_coef.clear();
     for (int k = j + 1; k < j + pc; ++k) {
-      double zz = red.dot(v[j], v[k], n, s);
-      axpy(v[k], v[j], -zz, n, s);
+      const double zz = tmp[1 + p + (k - j - 1)] * iz;
+      gs_vecs.push_back(v[k]);
+      gs_coef.push_back(zz);
       if (k >= pc) T(j, k - pc) = zz;
     }
+    mops.scale_sub(v[j], iz, gs_vecs, gs_coef, n, s);
     v[j + pc] = get();
     QCMG_CUDA(cudaMemsetAsync(v[j + pc], 0, n * 8, s));
     matvec(H, v[j], v[j + pc], true);
@@ -415,10 +467,15 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
       k0 = j - pc;
       if (defl[k0 - 1] == 0) erase(k0 - 1);
     }
+    // v_{j+pc} -= sum_k T(k, j) v_k over the band (one kernel)
+    rec_vecs.clear();
+    rec_coef.clear();
     for (int k = k0; k < j; ++k) {
       T(k, j) = T(j, k);
-      axpy(v[j + pc], v[k], -T(k, j), n, s);
+      rec_vecs.push_back(v[k]);
+      rec_coef.push_back(T(k, j));
     }
+    mops.multiaxpy(rec_vecs, rec_coef, v[j + pc], n, s);
     for (int idx : I) {
       double w = red.dot(v[idx], v[j + pc], n, s);
       axpy(v[j + pc], v[idx], -w, n, s);
