@@ -418,6 +418,66 @@ def run_cpt(args):
                                              "eta=0.1"}}))
 
 
+def cdmft_instances(n, n_bath, seed=0):
+    """Seeded CDMFT instances of the batched-CDMFT config: U ~ U[0,12],
+    mu ~ U[0,U], bath energies ~ U[-3,3], hybridizations ~ U[0,1] (t = 1,
+    t' = 0)."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        U = rng.uniform(0, 12)
+        mu = rng.uniform(0, U)
+        eb = rng.uniform(-3, 3, n_bath)
+        tb = rng.uniform(0, 1, n_bath)
+        out.append((U, mu, eb, tb))
+    return out
+
+
+def run_cdmft(args):
+    """CDMFT loops of the plaquette + bath model to convergence, one after the
+    other on the device: converged points per hour."""
+    import numpy as np
+    import torch
+    from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model
+    torch.cuda.set_device(0)
+    nb = args.bath
+    sector = {4: "R0:N8:S0", 8: "R0:N12:S0"}[nb]
+    names = bath_names(nb)
+    rows = []
+    t_all = time.perf_counter()
+    for U, mu, eb, tb in cdmft_instances(args.samples, nb, seed=args.seed):
+        lm = plaquette_bath_model(nb, sector)
+        params = {"t": 1.0, "tp": 0.0, "U": U, "mu": mu}
+        params.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
+        lm.set_parameters(params)
+        c = CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64)
+        t0 = time.perf_counter()
+        ok, why = True, ""
+        try:
+            c.run()
+        except Exception as e:  # a failed instance is reported, the others still run
+            ok, why = False, f"{type(e).__name__}: {e}"[:160]
+        rows.append((ok, max(c.niter, len(c.history)), time.perf_counter() - t0, c.time_ed,
+                     c.time_fit, c.dist, why))
+    total = time.perf_counter() - t_all
+    conv = [r for r in rows if r[0]]
+    failures = sorted({r[6] for r in rows if not r[0]})
+    print(json.dumps({
+        "metric": "cdmft_converged_points_per_hour", "value": len(conv) / total * 3600.0,
+        "unit": "points/h", "higher_is_better": True, "samples": len(rows),
+        "converged": len(conv), "mean_iterations": float(np.mean([r[1] for r in rows])),
+        "s_per_point": total / max(len(rows), 1),
+        "s_per_iteration": sum(r[2] for r in rows) / max(sum(r[1] for r in rows), 1),
+        "impurity_and_host_s": sum(r[3] for r in rows), "bath_fit_s": sum(r[4] for r in rows),
+        "failures": failures, "iteration": "broyden",
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"2x2 plaquette + {nb} bath orbitals, sector {sector}, "
+                               f"200 Matsubara frequencies (beta=50), 64x64 k grid, "
+                               f"Broyden CDMFT to the parameters test (1e-4)",
+                   "instances": "seeded U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -429,8 +489,13 @@ def main():
                     help="NXxNY Hubbard cluster at half filling (profiling of smaller cases)")
     ap.add_argument("--electrons", type=int, default=None,
                     help="electrons in the sector (default: half filling)")
-    ap.add_argument("--workload", default="product", choices=["product", "lanczos", "sef", "cpt"],
+    ap.add_argument("--workload", default="product",
+                    choices=["product", "lanczos", "sef", "cpt", "cdmft"],
                     help="product (the headline line) or one of the secondary measurements")
+    ap.add_argument("--bath", type=int, default=8, choices=[4, 8],
+                    help="bath orbitals of the CDMFT workload")
+    ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
+    ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
     args = ap.parse_args()
     global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))
@@ -443,6 +508,8 @@ def main():
         run_sef(args)
     elif args.workload == "cpt":
         run_cpt(args)
+    elif args.workload == "cdmft":
+        run_cdmft(args)
     else:
         run_gpu(args)
 

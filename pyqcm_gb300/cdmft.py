@@ -1,0 +1,291 @@
+"""CDMFT self-consistency on the engine.
+
+Restates the reference's CDMFT procedure (pyqcm/cdmft.py):
+- the Matsubara frequency grid (frequency_grid('matsubara'), cdmft.py:846-851
+  and :869, CDMFT weights 1);
+- the 'parameters' convergence test of depth 2 (convergence_manager,
+  cdmft.py:14-106);
+- one CDMFT step (CDMFT_step, cdmft.py:479-628): solve the impurity problem
+  (ground state + Green function on the device), build the host function
+  G_host(iw) on the k grid (device), then fit the bath parameters so that the
+  hybridization function matches -G_host;
+- the bath fit by least squares on the residuals
+  r_n = sqrt(w_n) (Gamma(iw_n) + G_host(iw_n)), real and imaginary parts
+  (CDMFT_residuals, src_qcm/CPT.cpp:556-610), with scipy's 'trf' solver and
+  the reference's tolerances (optimize(method='trf'), cdmft.py:1539-1640);
+- the outer fixed-point iteration with damping (fixed_point_iteration,
+  pyqcm/__init__.py:2773-2845).
+
+Differences: the Jacobian of the residuals is exact (Gamma = theta (z - E)^-1
+theta^T is linear in the bath parameters through theta and E) instead of the
+reference's central differences (CPT.cpp:616-672), and the residuals are
+stacked row-major per frequency (the reference's matrix storage order);
+neither changes the least-squares optimum.
+"""
+import time
+
+import numpy as np
+
+from . import lattice as lat
+from .ed import ClusterModel
+
+
+def matsubara_grid(wc, beta):
+    """(frequencies, integration weights, CDMFT weights) of the Matsubara grid
+    up to wc at inverse temperature beta (cdmft.py:846-851, :869)."""
+    wr = np.arange(np.pi / beta, wc + 1e-6, 2 * np.pi / beta)
+    return wr, (2 * np.pi / beta) * np.ones_like(wr), np.ones_like(wr)
+
+
+class ConvergenceManager:
+    """The 'parameters' test: converged when |x - x_k| / n < tol for each of
+    the depth previous iterates (cdmft.py:14-106)."""
+
+    def __init__(self, tol, depth=2):
+        self.tol, self.depth = tol, depth
+        self.X = []
+
+    def test(self, x):
+        x = np.array(x, np.float64)
+        if len(self.X) < self.depth:
+            self.X.append(x)
+            return False
+        ok = all(np.linalg.norm(x - y) / x.shape[0] <= self.tol for y in self.X)
+        self.X = self.X[1:] + [x]
+        return ok
+
+
+class BathFit:
+    """Residuals of the bath fit and their exact Jacobian, for the cluster
+    parameters `names` (cluster names: 'eb1', 'tb1', ...) of cluster model cm
+    at fixed other parameter values `values`."""
+
+    def __init__(self, cm, values, names, freqs, weights, host, spin_down=False):
+        self.ns = cm.n_sites
+        self.names = list(names)
+        fixed = {k: v for k, v in values.items() if k not in self.names}
+        T0 = cm.one_body_matrix(fixed, spin_down)
+        self.theta0, self.E0 = T0[:self.ns, self.ns:], T0[self.ns:, self.ns:]
+        self.dtheta, self.dE = [], []
+        for n in self.names:  # the blocks are linear in each parameter
+            Tp = cm.one_body_matrix({n: 1.0}, spin_down)
+            self.dtheta.append(Tp[:self.ns, self.ns:])
+            self.dE.append(Tp[self.ns:, self.ns:])
+        self.iw = 1j * np.asarray(freqs, np.float64)
+        self.sw = np.sqrt(np.asarray(weights, np.float64))
+        self.host = np.asarray(host, np.complex128)
+        self.nb = self.E0.shape[0]
+
+    def blocks(self, x):
+        th = self.theta0.copy()
+        E = self.E0.copy()
+        for xp, dth, dE in zip(x, self.dtheta, self.dE):
+            th += xp * dth
+            E += xp * dE
+        return th, E
+
+    def _resolvent(self, E):
+        eye = np.eye(self.nb)
+        return np.linalg.inv(self.iw[:, None, None] * eye[None] - E[None])
+
+    def gamma(self, x):
+        th, E = self.blocks(x)
+        R = self._resolvent(E)
+        return th[None] @ R @ th.T[None]
+
+    def _pack(self, Z):
+        Z = self.sw[:, None, None] * Z
+        return np.concatenate([Z.real.reshape(len(Z), -1), Z.imag.reshape(len(Z), -1)], axis=1).ravel()
+
+    def residuals(self, x):
+        return self._pack(self.gamma(x) + self.host)
+
+    def jacobian(self, x):
+        th, E = self.blocks(x)
+        R = self._resolvent(E)
+        RthT = R @ th.T[None]           # (nw, nb, ns)
+        thR = th[None] @ R               # (nw, ns, nb)
+        cols = []
+        for dth, dE in zip(self.dtheta, self.dE):
+            d = dth[None] @ RthT + thR @ dth.T[None] + thR @ dE[None] @ RthT
+            cols.append(self._pack(d))
+        return np.stack(cols, axis=1)
+
+    def distance(self, x, normal=True):
+        """sum_n w_n |Gamma + G_host|^2 (x2 normal mixing) dw / dim^2, the
+        reference's reporting scale (CPT.cpp:519-555) with CDMFT weights."""
+        Z = self.gamma(x) + self.host
+        w = self.sw ** 2
+        d = float(np.sum(w[:, None, None] * np.abs(Z) ** 2))
+        if normal:
+            d *= 2
+        dw = float(self.iw[1].imag - self.iw[0].imag) if len(self.iw) > 1 else 1.0
+        return d * dw / (self.ns * self.ns)
+
+
+def fit_bath(fit, x0, accur_bath=1e-6, accur_dist=1e-8, max_nfev=2000):
+    """scipy least_squares 'trf' with the reference's tolerances
+    (optimize(method='trf'), cdmft.py:1588-1603)."""
+    import scipy.optimize
+    sol = scipy.optimize.least_squares(fit.residuals, np.asarray(x0, np.float64), jac=fit.jacobian,
+                                       method="trf", max_nfev=max_nfev, ftol=accur_dist,
+                                       xtol=accur_bath, gtol=1e-12)
+    return sol.x, sol.nfev
+
+
+class CDMFT:
+    """The CDMFT loop on a lattice model (pyqcm.cdmft.CDMFT with
+    iteration='fixed_point', convergence='parameters', method='trf').
+
+    varia: lattice-level bath parameter names of cluster 1 ('eb1_1', ...).
+    grid: (wc, beta) of the Matsubara grid.  kside: side of the k grid of the
+    host function.  x0: starting bath parameters (default: the model's)."""
+
+    def __init__(self, model, varia, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=32,
+                 miniter=0, depth=2, accur=1e-4, accur_bath=1e-6, accur_dist=1e-8, damping=0.0,
+                 max_nfev=2000, x0=None, iteration="broyden", verbose=False):
+        if iteration not in ("broyden", "fixed_point"):
+            raise ValueError("iteration must be 'broyden' or 'fixed_point'")
+        self.iteration = iteration
+        self.model = model
+        self.varia = list(varia)
+        self.cnames = [v[:-2] if v.endswith("_1") else v for v in self.varia]
+        self.wr, _, self.cw = matsubara_grid(*grid)
+        self.kside = kside
+        self.maxiter, self.miniter = maxiter, miniter
+        self.conv = ConvergenceManager(accur, depth)
+        self.accur_bath, self.accur_dist, self.max_nfev = accur_bath, accur_dist, max_nfev
+        self.damping = damping
+        self.verbose = verbose
+        if x0 is None:
+            x0 = [model.params[v] for v in self.varia]
+        self.x = np.array(x0, np.float64)
+        self.niter = 0
+        self.dist = None
+        self.history = []
+        self.time_ed = self.time_fit = 0.0
+
+    def step(self, x):
+        """One CDMFT step from bath x: returns the fitted bath."""
+        params = dict(self.model.params)
+        params.update({v: float(xv) for v, xv in zip(self.varia, x)})
+        self.model.set_parameters(params)
+        t0 = time.perf_counter()
+        inst = self.model.instance()
+        host = inst.CDMFT_host(self.wr, self.cw, kside=self.kside)
+        t1 = time.perf_counter()
+        values = dict(inst.cluster.values)
+        newx = np.array(x, np.float64)
+        dist = 0.0
+        normal = not (inst.cluster.mixing & 4)
+        for sd, H in host.items():
+            fit = BathFit(self.model.cluster, values, self.cnames, self.wr, self.cw, H, sd)
+            newx, _ = fit_bath(fit, newx, self.accur_bath, self.accur_dist, self.max_nfev)
+            dist += fit.distance(newx, normal)
+        t2 = time.perf_counter()
+        self.time_ed += t1 - t0
+        self.time_fit += t2 - t1
+        self.dist = dist
+        self.E0 = inst.cluster.E0
+        return newx
+
+    def run(self):
+        """Iterates to self-consistency (Broyden or fixed point, as the
+        reference's CDMFT does) until the fitted bath passes the parameters
+        test; returns the converged bath."""
+        if self.iteration == "broyden":
+            self._broyden()
+        else:
+            self._fixed_point()
+        params = dict(self.model.params)
+        params.update({v: float(xv) for v, xv in zip(self.varia, self.x)})
+        self.model.set_parameters(params)
+        return self.x
+
+    def _fixed_point(self):
+        """x <- step(x), damped (fixed_point_iteration, pyqcm/__init__.py:2773-2845)."""
+        x0 = self.x.copy()
+        it = 0
+        while True:
+            xs = self.step(x0)
+            x = xs + self.damping * (x0 - xs)   # (alpha - 1) F(x0) + x0, F = x0 - step(x0)
+            it += 1
+            self.history.append(xs.copy())
+            if self.verbose:
+                print(f"CDMFT iteration {it}: |dx| = {np.linalg.norm(x - x0):.3g}, "
+                      f"distance = {self.dist:.3g}")
+            x0 = x
+            if self.conv.test(xs) and it >= self.miniter:
+                break
+            if it > self.maxiter:
+                raise RuntimeError(f"CDMFT did not converge in {self.maxiter} iterations")
+        self.x = x0
+        self.niter = it
+
+    def _broyden(self):
+        """Broyden's root search on F(x) = x - step(x) with the inverse-Jacobian
+        update of pyqcm.broyden (pyqcm/__init__.py, broyden), initial inverse
+        Jacobian (1 + damping) * identity; the parameters test runs on the
+        fitted bath of each step."""
+        n = len(self.x)
+        I = (1.0 + self.damping) * np.eye(n)
+        F = lambda x: x - self._step_record(x)
+        x = self.x.copy()
+        f0 = F(x)
+        f = f0.copy()
+        it = 0
+        while True:
+            dx = -I @ f
+            if np.any(np.isnan(dx)):
+                raise RuntimeError("NaN produced in the Broyden iteration")
+            x = x + dx
+            if self.verbose:
+                print(f"CDMFT Broyden iteration {it + 1}: |dx| = {np.linalg.norm(dx):.3g}, "
+                      f"distance = {self.dist:.3g}")
+            if np.linalg.norm(dx) < 1e-6 and it >= self.miniter:
+                self.conv.test(self.xs)
+                break
+            if self.conv.test(self.xs) and it >= self.miniter:
+                break
+            f = F(x)
+            df = f - f0
+            f0 = f.copy()
+            I += np.outer(dx - I @ df, dx) @ I / (dx @ (I @ df))
+            it += 1
+            if it > self.maxiter:
+                raise RuntimeError(f"CDMFT did not converge in {self.maxiter} iterations")
+        self.x = x
+        self.niter = it + 1
+
+    def _step_record(self, x):
+        self.xs = self.step(x)
+        self.history.append(self.xs.copy())
+        return self.xs
+
+
+def plaquette_bath_model(n_bath=8, sector="R0:N12:S0"):
+    """The 2x2 plaquette with n_bath bath orbitals on the square lattice
+    (bath k: energy eb{k+1}, hybridization tb{k+1} with site k % 4), with
+    lattice operators t (nearest neighbour), tp (diagonal), U and the built-in
+    mu: the CDMFT benchmark model (BASELINE configs' batched CDMFT case with
+    one hybridization per bath orbital)."""
+    from .lattice import LatticeModel
+    ns, no = 4, 4 + n_bath
+    cm = ClusterModel(ns, n_bath)
+    for k in range(n_bath):
+        b, s = ns + k, k % ns
+        cm.new_operator(f"eb{k+1}", "one-body", [(b, b, 1.0), (b + no, b + no, 1.0)])
+        cm.new_operator(f"tb{k+1}", "one-body", [(s, b, 1.0), (s + no, b + no, 1.0)])
+    lm = LatticeModel(cm, [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)], [(2, 0, 0), (0, 2, 0)])
+    lm.interaction_operator("U", 1.0)
+    lm.hopping_operator("t", (1, 0, 0), -1.0)
+    lm.hopping_operator("t", (0, 1, 0), -1.0)
+    lm.hopping_operator("tp", (1, 1, 0), -1.0)
+    lm.hopping_operator("tp", (-1, 1, 0), -1.0)
+    lm.set_target_sectors(sector)
+    return lm
+
+
+def bath_names(n_bath):
+    """Lattice-level names of the bath parameters of plaquette_bath_model."""
+    return [f"eb{k+1}_1" for k in range(n_bath)] + [f"tb{k+1}_1" for k in range(n_bath)]
