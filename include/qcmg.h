@@ -264,6 +264,32 @@ int qcmg_cpt_periodized(qcmg_lattice* lat, int nz, const double* z, int nk, cons
 int qcmg_cdmft_projected(qcmg_lattice* lat, int nw, const double* w, int kside, int dimk,
                          double* pgf);
 
+/* ---------------------------------------------------------------------------
+ * Multilayer perceptron of the learned CDMFT warm start (no counterpart in
+ * the reference).  Layers l < n_layers map width[l] -> width[l+1]; hidden
+ * layers use tanh, the last one is linear.  Parameters are FP32 on the host
+ * side of the ABI, laid out W_0, b_0, W_1, b_1, ... with W_l row-major
+ * [width[l+1] x width[l]]; the device keeps an FP32 master copy and uses a
+ * BF16 copy of the weights in every product, accumulating in FP32.  All
+ * arrays below are host arrays, row-major [batch x width]. */
+typedef struct qcmg_mlp qcmg_mlp;
+
+int qcmg_mlp_create(int n_layers, const int* widths, qcmg_mlp** out);
+int qcmg_mlp_destroy(qcmg_mlp* mlp);
+int qcmg_mlp_num_params(qcmg_mlp* mlp, size_t* n);
+/* Sets the FP32 master parameters (and their BF16 copy); resets Adam. */
+int qcmg_mlp_set_params(qcmg_mlp* mlp, const float* params);
+int qcmg_mlp_get_params(qcmg_mlp* mlp, float* params);
+int qcmg_mlp_forward(qcmg_mlp* mlp, int batch, const float* x, float* y);
+/* Mean squared error against t and its gradient with respect to the FP32
+ * parameters (grad may be NULL). */
+int qcmg_mlp_loss_grad(qcmg_mlp* mlp, int batch, const float* x, const float* t, float* loss,
+                       float* grad);
+/* Adam (beta1 0.9, beta2 0.999, eps 1e-8) over `epochs` shuffled passes of
+ * minibatches of `batch` rows; *final_loss = mean loss of the last epoch. */
+int qcmg_mlp_train(qcmg_mlp* mlp, int n, const float* x, const float* t, int epochs, int batch,
+                   float lr, unsigned seed, float* final_loss);
+
 #ifdef __cplusplus
 }
 #endif

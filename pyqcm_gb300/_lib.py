@@ -68,6 +68,15 @@ SIGNATURES = {
     "qcmg_sef_grid": (c_int, [vp, c_int, vp, vp, c_int, c_int, c_int, dbl_p]),
     "qcmg_cpt_periodized": (c_int, [vp, c_int, vp, c_int, vp, vp]),
     "qcmg_cdmft_projected": (c_int, [vp, c_int, vp, c_int, c_int, vp]),
+    "qcmg_mlp_create": (c_int, [c_int, vp, ctypes.POINTER(vp)]),
+    "qcmg_mlp_destroy": (c_int, [vp]),
+    "qcmg_mlp_num_params": (c_int, [vp, size_p]),
+    "qcmg_mlp_set_params": (c_int, [vp, vp]),
+    "qcmg_mlp_get_params": (c_int, [vp, vp]),
+    "qcmg_mlp_forward": (c_int, [vp, c_int, vp, vp]),
+    "qcmg_mlp_loss_grad": (c_int, [vp, c_int, vp, vp, vp, vp]),
+    "qcmg_mlp_train": (c_int, [vp, c_int, vp, vp, c_int, c_int, ctypes.c_float, ctypes.c_uint,
+                               vp]),
 }
 
 
