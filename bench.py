@@ -478,6 +478,40 @@ def run_cdmft(args):
                    "instances": "seeded U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}))
 
 
+def run_warmstart(args):
+    """The learned warm start: train the device MLP on converged CDMFT solves,
+    then run CDMFT on held-out points from the default bath and from the
+    network's prediction; wall time and iterations of both."""
+    import numpy as np
+    import torch
+    from pyqcm_gb300 import warmstart as ws
+    torch.cuda.set_device(0)
+    nb = args.bath
+    path = args.warm_data or os.path.join(ROOT, "pyqcm_gb300", "data", f"warmstart_{nb}bath_train.npz")
+    P, Y = ws.load(path)
+    t0 = time.perf_counter()
+    m, loss = ws.train(P, Y, epochs=args.epochs)
+    t_train = time.perf_counter() - t0
+    Ptest = ws.sample_params(args.samples, seed=args.seed + 1000)  # held out: another seed
+    res = ws.evaluate(m, Ptest, nb)
+    s_plain = sum(r["s_plain"] for r in res)
+    s_warm = sum(r["s_warm"] for r in res)
+    print(json.dumps({
+        "metric": "cdmft_warm_start_speedup", "value": s_plain / s_warm, "unit": "x",
+        "higher_is_better": True, "held_out": len(res), "train_points": len(P),
+        "train_loss": loss, "train_s": t_train,
+        "mean_iterations_plain": float(np.mean([r["iters_plain"] for r in res])),
+        "mean_iterations_warm": float(np.mean([r["iters_warm"] for r in res])),
+        "s_plain": s_plain, "s_warm": s_warm,
+        "max_bath_difference": float(max(r["max_dx"] for r in res)),
+        "median_prediction_error": float(np.median([r["pred_err"] for r in res])),
+        "fallbacks": int(sum(r["fallback"] for r in res)),
+        "dtype": "bf16 weights, f32 accumulate (MLP); f64 (CDMFT)", "data": "synthetic",
+        "config": {"workload": f"2x2 plaquette + {nb} baths, MLP 4-256-256-{2 * nb}, "
+                               "U in [4,12], t' in [-0.4,0], mu in [0.35U,0.5U]",
+                   "convergence": "parameters test 1e-4 (Broyden)"}}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -490,12 +524,14 @@ def main():
     ap.add_argument("--electrons", type=int, default=None,
                     help="electrons in the sector (default: half filling)")
     ap.add_argument("--workload", default="product",
-                    choices=["product", "lanczos", "sef", "cpt", "cdmft"],
+                    choices=["product", "lanczos", "sef", "cpt", "cdmft", "warmstart"],
                     help="product (the headline line) or one of the secondary measurements")
     ap.add_argument("--bath", type=int, default=8, choices=[4, 8],
                     help="bath orbitals of the CDMFT workload")
     ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
+    ap.add_argument("--warm-data", default=None, help="training set of the warm-start workload")
+    ap.add_argument("--epochs", type=int, default=3000, help="training epochs of the warm-start MLP")
     args = ap.parse_args()
     global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))
@@ -510,6 +546,8 @@ def main():
         run_cpt(args)
     elif args.workload == "cdmft":
         run_cdmft(args)
+    elif args.workload == "warmstart":
+        run_warmstart(args)
     else:
         run_gpu(args)
 
