@@ -531,7 +531,7 @@ def main():
     ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
     ap.add_argument("--warm-data", default=None, help="training set of the warm-start workload")
-    ap.add_argument("--epochs", type=int, default=3000, help="training epochs of the warm-start MLP")
+    ap.add_argument("--epochs", type=int, default=20000, help="training epochs of the warm-start MLP")
     args = ap.parse_args()
     global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))
