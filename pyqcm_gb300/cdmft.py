@@ -71,6 +71,19 @@ class BathFit:
             Tp = cm.one_body_matrix({n: 1.0}, spin_down)
             self.dtheta.append(Tp[:self.ns, self.ns:])
             self.dE.append(Tp[self.ns:, self.ns:])
+        # each parameter enters theta and E through a few entries only:
+        # (parameter, row, column, value) of every nonzero entry
+        def entries(mats):
+            out = [(p, r, c, m[r, c]) for p, m in enumerate(mats) for r, c in zip(*np.nonzero(m))]
+            cols = list(zip(*out)) if out else [(), (), (), ()]
+            return (np.array(cols[0], np.intp), np.array(cols[1], np.intp),
+                    np.array(cols[2], np.intp), np.array(cols[3], np.float64))
+        self.nz_theta = entries(self.dtheta)
+        self.nz_E = entries(self.dE)
+        # fancy-index += is exact when no target repeats; np.add.at otherwise
+        pa = set(zip(self.nz_theta[0].tolist(), self.nz_theta[1].tolist()))
+        self.theta_unique = len(pa) == len(self.nz_theta[0])
+        self.E_unique = len(set(self.nz_E[0].tolist())) == len(self.nz_E[0])
         self.iw = 1j * np.asarray(freqs, np.float64)
         self.sw = np.sqrt(np.asarray(weights, np.float64))
         self.host = np.asarray(host, np.complex128)
@@ -84,14 +97,21 @@ class BathFit:
             E += xp * dE
         return th, E
 
-    def _resolvent(self, E):
+    def _sandwich(self, th, E):
+        """(theta R, R theta^T) per frequency, R = (iw - E)^-1.  A diagonal
+        bath (the usual case: bath energies only) needs no inverse."""
+        if not np.count_nonzero(E - np.diag(np.diag(E))):
+            r = 1.0 / (self.iw[:, None] - np.diag(E)[None, :])      # (nw, nb)
+            thR = th[None, :, :] * r[:, None, :]
+            return thR, thR.transpose(0, 2, 1)
         eye = np.eye(self.nb)
-        return np.linalg.inv(self.iw[:, None, None] * eye[None] - E[None])
+        R = np.linalg.inv(self.iw[:, None, None] * eye[None] - E[None])
+        return th[None] @ R, R @ th.T[None]
 
     def gamma(self, x):
         th, E = self.blocks(x)
-        R = self._resolvent(E)
-        return th[None] @ R @ th.T[None]
+        thR, _ = self._sandwich(th, E)
+        return thR @ th.T[None]
 
     def _pack(self, Z):
         Z = self.sw[:, None, None] * Z
@@ -102,14 +122,33 @@ class BathFit:
 
     def jacobian(self, x):
         th, E = self.blocks(x)
-        R = self._resolvent(E)
-        RthT = R @ th.T[None]           # (nw, nb, ns)
-        thR = th[None] @ R               # (nw, ns, nb)
-        cols = []
-        for dth, dE in zip(self.dtheta, self.dE):
-            d = dth[None] @ RthT + thR @ dth.T[None] + thR @ dE[None] @ RthT
-            cols.append(self._pack(d))
-        return np.stack(cols, axis=1)
+        thR, RthT = self._sandwich(th, E)   # (nw, ns, nb), (nw, nb, ns)
+        # d_p = dth_p R th^T + th R dth_p^T + th R dE_p R th^T, from the few
+        # nonzero entries of dth_p and dE_p (no small dense products)
+        n, nw, ns = len(self.names), thR.shape[0], self.ns
+        d = np.zeros((n, nw, ns, ns), np.complex128)
+        P, A, B, V = self.nz_theta
+        if len(P):
+            t1 = V[:, None, None] * RthT[:, B, :].transpose(1, 0, 2)    # (nnz, w, c)
+            t2 = V[:, None, None] * thR[:, :, B].transpose(2, 0, 1)     # (nnz, w, a)
+            if self.theta_unique:
+                d[P, :, A, :] += t1
+                d[P, :, :, A] += t2
+            else:
+                np.add.at(d, (P, slice(None), A, slice(None)), t1)
+                np.add.at(d, (P, slice(None), slice(None), A), t2)
+        P, B, E3, V = self.nz_E
+        if len(P):
+            t3 = (V[:, None, None, None] * thR[:, :, B].transpose(2, 0, 1)[:, :, :, None]
+                  * RthT[:, E3, :].transpose(1, 0, 2)[:, :, None, :])
+            if self.E_unique:
+                d[P] += t3
+            else:
+                np.add.at(d, P, t3)
+        d *= self.sw[None, :, None, None]
+        cols = np.concatenate([d.real.reshape(n, d.shape[1], -1), d.imag.reshape(n, d.shape[1], -1)],
+                              axis=2)
+        return cols.reshape(n, -1).T
 
     def distance(self, x, normal=True):
         """sum_n w_n |Gamma + G_host|^2 (x2 normal mixing) dw / dim^2, the

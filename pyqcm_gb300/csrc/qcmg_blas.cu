@@ -67,6 +67,16 @@ __global__ void k_axpy(double* __restrict__ y, const double* __restrict__ x, dou
     y[i] = fma(a, x[i], y[i]);
 }
 
+// y -= a x with a read from device memory (a scalar left there by a
+// reduction, so the host need not wait for it).
+__global__ void k_axpy_neg_dev(double* __restrict__ y, const double* __restrict__ x,
+                               const double* __restrict__ a, size_t n) {
+  const double c = -*a;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    y[i] = fma(c, x[i], y[i]);
+}
+
 __global__ void k_scale2(double* __restrict__ r, double s1, double* __restrict__ q, double s2,
                          size_t n) {
   for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
@@ -143,6 +153,21 @@ double Reducer::axpy_norm2(double* r, const double* q, double alpha, size_t n, c
   QCMG_CUDA(cudaMemcpyAsync(host, out.p, sizeof(double), cudaMemcpyDeviceToHost, s));
   QCMG_CUDA(cudaStreamSynchronize(s));
   return host[0];
+}
+
+void Reducer::dot_dev(const double* x, const double* y, size_t n, double* out_dev,
+                      cudaStream_t s) {
+  if (!part.p) init();
+  unsigned g = red_grid(n);
+  k_dot_partial<<<g, kRedThreads, 0, s>>>(x, y, n, part.p);
+  k_reduce_final<<<1, kRedBlocks, 0, s>>>(part.p, (int)g, out_dev);
+  QCMG_CUDA(cudaGetLastError());
+}
+
+void axpy_neg_dev(double* y, const double* x, const double* a_dev, size_t n, cudaStream_t s) {
+  if (!n) return;
+  k_axpy_neg_dev<<<ew_grid(n), 256, 0, s>>>(y, x, a_dev, n);
+  QCMG_CUDA(cudaGetLastError());
 }
 
 void axpy(double* y, const double* x, double a, size_t n, cudaStream_t s) {

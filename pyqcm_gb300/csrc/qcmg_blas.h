@@ -19,11 +19,16 @@ struct Reducer {
   ~Reducer();
   void init();
   double dot(const double* x, const double* y, size_t n, cudaStream_t s);
+  // x . y (same partials and summation order as dot) written to out_dev,
+  // without a host round trip.
+  void dot_dev(const double* x, const double* y, size_t n, double* out_dev, cudaStream_t s);
   // r -= alpha q; returns |r|^2.
   double axpy_norm2(double* r, const double* q, double alpha, size_t n, cudaStream_t s);
 };
 
 void axpy(double* y, const double* x, double a, size_t n, cudaStream_t s);
+// y -= (*a_dev) x, bitwise the same as axpy(y, x, -(*a_dev), ...).
+void axpy_neg_dev(double* y, const double* x, const double* a_dev, size_t n, cudaStream_t s);
 void scale2(double* r, double s1, double* q, double s2, size_t n, cudaStream_t s);
 void scale(double* x, double a, size_t n, cudaStream_t s);
 void replay_step(double* r, double* q, double* gs, double alpha, double beta, double c, size_t n,

@@ -22,10 +22,28 @@ namespace qcmg {
 
 constexpr int kTile = 2048;  // elements of w staged per block iteration
 
+// Vector lists and coefficients passed to the kernels by value (up to
+// kByValue entries): no host-to-device copy of a pointer array per call,
+// which on small sectors costs more than the kernel.  Longer lists go
+// through device arrays (the same kernels, instantiated on pointers).
+constexpr int kByValue = 64;
+struct VecList {
+  const double* v[kByValue];
+  __device__ const double* operator[](int k) const { return v[k]; }
+};
+struct MutVecList {
+  double* v[kByValue];
+  __device__ double* operator[](int k) const { return v[k]; }
+};
+struct CoefList {
+  double c[kByValue];
+  __device__ double operator[](int k) const { return c[k]; }
+};
+
 // part[b*m + k] = sum over block b's tiles of V_k . w
-__global__ void __launch_bounds__(256) k_multidot(const double* const* __restrict__ V, int m,
-                                                  const double* __restrict__ w, size_t n,
-                                                  double* __restrict__ part) {
+template <class VL>
+__global__ void __launch_bounds__(256) k_multidot(VL V, int m, const double* __restrict__ w,
+                                                  size_t n, double* __restrict__ part) {
   __shared__ double ws[kTile];
   extern __shared__ double acc[];  // m accumulators
   for (int k = threadIdx.x; k < m; k += blockDim.x) acc[k] = 0.0;
@@ -59,9 +77,9 @@ __global__ void k_multidot_final(const double* __restrict__ part, int nb, int m,
 }
 
 // w -= sum_k c_k V_k
-__global__ void __launch_bounds__(256) k_multiaxpy(const double* const* __restrict__ V, int m,
-                                                   const double* __restrict__ c,
-                                                   double* __restrict__ w, size_t n) {
+template <class VL, class CL>
+__global__ void __launch_bounds__(256) k_multiaxpy(VL V, int m, CL c, double* __restrict__ w,
+                                                   size_t n) {
   extern __shared__ double cs[];
   for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = c[k];
   __syncthreads();
@@ -75,9 +93,9 @@ __global__ void __launch_bounds__(256) k_multiaxpy(const double* const* __restri
 
 // v <- sc * v, then V_k <- V_k - c_k * v for k < m (the scaled v): one pass
 // over v for the whole Gram-Schmidt sweep of a band-Lanczos step.
-__global__ void __launch_bounds__(256) k_scale_sub(double* __restrict__ v, double sc,
-                                                   double* const* __restrict__ V,
-                                                   const double* __restrict__ c, int m, size_t n) {
+template <class VL, class CL>
+__global__ void __launch_bounds__(256) k_scale_sub(double* __restrict__ v, double sc, VL V, CL c,
+                                                   int m, size_t n) {
   extern __shared__ double cs[];
   for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = c[k];
   __syncthreads();
@@ -100,7 +118,7 @@ int multidot_blocks(size_t n) {
 void multidot_launch(int m, const double* const* V, const double* w, size_t n, double* part,
                      double* out, cudaStream_t s) {
   const int nb = multidot_blocks(n);
-  k_multidot<<<nb, 256, m * sizeof(double), s>>>(V, m, w, n, part);
+  k_multidot<const double* const*><<<nb, 256, m * sizeof(double), s>>>(V, m, w, n, part);
   k_multidot_final<<<(m + 127) / 128, 128, 0, s>>>(part, nb, m, out);
   QCMG_CUDA(cudaGetLastError());
 }
@@ -115,29 +133,48 @@ struct MultiOps {
     const int m = (int)V.size();
     out.assign(m, 0.0);
     if (m == 0) return;
-    nblocks = (int)std::min<size_t>((n + kTile - 1) / kTile, 2 * 152);
-    if (nblocks < 1) nblocks = 1;
-    ptrs.alloc(m);
-    QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+    nblocks = multidot_blocks(n);
     part.alloc((size_t)nblocks * m);
     coef.alloc(m);
-    k_multidot<<<nblocks, 256, m * sizeof(double), s>>>(ptrs.p, m, w, n, part.p);
+    if (m <= kByValue) {
+      VecList L;
+      for (int k = 0; k < m; ++k) L.v[k] = V[k];
+      k_multidot<VecList><<<nblocks, 256, m * sizeof(double), s>>>(L, m, w, n, part.p);
+    } else {
+      ptrs.alloc(m);
+      QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+      k_multidot<const double* const*>
+          <<<nblocks, 256, m * sizeof(double), s>>>(ptrs.p, m, w, n, part.p);
+    }
     k_multidot_final<<<(m + 127) / 128, 128, 0, s>>>(part.p, nblocks, m, coef.p);
     QCMG_CUDA(cudaGetLastError());
     QCMG_CUDA(cudaMemcpyAsync(out.data(), coef.p, m * sizeof(double), cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
   }
+  static unsigned elementwise_grid(size_t n) {
+    return (unsigned)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 8));
+  }
   void multiaxpy(const std::vector<const double*>& V, const std::vector<double>& c, double* w,
                  size_t n, cudaStream_t s) {
     const int m = (int)V.size();
     if (m == 0 || n == 0) return;
-    ptrs.alloc(m);
-    coef.alloc(m);
-    QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
-    QCMG_CUDA(cudaMemcpyAsync(coef.p, c.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
-    size_t g = std::min<size_t>((n + 255) / 256, 152 * 8);
-    k_multiaxpy<<<(unsigned)std::max<size_t>(g, 1), 256, m * sizeof(double), s>>>(ptrs.p, m,
-                                                                                   coef.p, w, n);
+    if (m <= kByValue) {
+      VecList L;
+      CoefList C;
+      for (int k = 0; k < m; ++k) {
+        L.v[k] = V[k];
+        C.c[k] = c[k];
+      }
+      k_multiaxpy<VecList, CoefList>
+          <<<elementwise_grid(n), 256, m * sizeof(double), s>>>(L, m, C, w, n);
+    } else {
+      ptrs.alloc(m);
+      coef.alloc(m);
+      QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
+      QCMG_CUDA(cudaMemcpyAsync(coef.p, c.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+      k_multiaxpy<const double* const*, const double*>
+          <<<elementwise_grid(n), 256, m * sizeof(double), s>>>(ptrs.p, m, coef.p, w, n);
+    }
     QCMG_CUDA(cudaGetLastError());
   }
   // v <- sc v;  V_k <- V_k - c_k v  (k_scale_sub)
@@ -147,15 +184,23 @@ struct MultiOps {
                  size_t n, cudaStream_t s) {
     const int m = (int)V.size();
     if (n == 0) return;
-    wptrs.alloc(std::max(m, 1));
-    wcoef.alloc(std::max(m, 1));
-    if (m) {
+    const size_t sh = std::max(m, 1) * sizeof(double);
+    if (m <= kByValue) {
+      MutVecList L;
+      CoefList C;
+      for (int k = 0; k < m; ++k) {
+        L.v[k] = V[k];
+        C.c[k] = c[k];
+      }
+      k_scale_sub<MutVecList, CoefList><<<elementwise_grid(n), 256, sh, s>>>(v, sc, L, C, m, n);
+    } else {
+      wptrs.alloc(m);
+      wcoef.alloc(m);
       QCMG_CUDA(cudaMemcpyAsync(wptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
       QCMG_CUDA(cudaMemcpyAsync(wcoef.p, c.data(), m * sizeof(double), cudaMemcpyHostToDevice, s));
+      k_scale_sub<double* const*, const double*>
+          <<<elementwise_grid(n), 256, sh, s>>>(v, sc, wptrs.p, wcoef.p, m, n);
     }
-    size_t g = std::min<size_t>((n + 255) / 256, 152 * 8);
-    k_scale_sub<<<(unsigned)std::max<size_t>(g, 1), 256, std::max(m, 1) * sizeof(double), s>>>(
-        v, sc, wptrs.p, wcoef.p, m, n);
     QCMG_CUDA(cudaGetLastError());
   }
 };
@@ -281,8 +326,7 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
   double* w = r.p;  // residual
   double ritz = 2.0 * tol;
   for (int j = 0; ritz > tol; ++j) {
-    QCMG_CUDA(cudaMemsetAsync(w, 0, n * 8, s));
-    matvec(H, V[j].p, w, true);
+    matvec(H, V[j].p, w, false);
     if (j > 0) axpy(w, V[j - 1].p, -res.beta.back(), n, s);
     double a = red.dot(V[j].p, w, n, s);
     res.alpha.push_back(a);
@@ -422,6 +466,31 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   std::vector<double> gs_coef;
   std::vector<const double*> rec_vecs;
   std::vector<double> rec_coef;
+  // The dots of the closing Gram-Schmidt sweep stay on the device: each
+  // lands in a slot of tdev (p + 1 slots per step), its axpy reads it there,
+  // and the host copies the slots into t only where t is read next (the
+  // convergence probe and the end), so a step waits on the device once.
+  const int slots = p + 1;
+  DevBuf<double> tdev;
+  tdev.alloc((size_t)M0 * slots);
+  std::vector<double> thost((size_t)M0 * slots);
+  struct Pending {
+    int slot, r, c;
+  };
+  std::vector<Pending> pend;
+  auto flush = [&]() {
+    if (pend.empty()) return;
+    int lo = pend.front().slot, hi = lo;
+    for (const Pending& q : pend) {
+      lo = std::min(lo, q.slot);
+      hi = std::max(hi, q.slot);
+    }
+    QCMG_CUDA(cudaMemcpyAsync(thost.data() + lo, tdev.p + lo, (size_t)(hi - lo + 1) * 8,
+                              cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+    for (const Pending& q : pend) T(q.r, q.c) = T(q.c, q.r) = thost[q.slot];
+    pend.clear();
+  };
   for (j = 0; j < M0; ++j) {
     // One multi-dot on the unscaled v_j gives its norm, its projections on
     // the p start vectors and its dots with the next pc-1 vectors (each of
@@ -460,8 +529,7 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
     }
     mops.scale_sub(v[j], iz, gs_vecs, gs_coef, n, s);
     v[j + pc] = get();
-    QCMG_CUDA(cudaMemsetAsync(v[j + pc], 0, n * 8, s));
-    matvec(H, v[j], v[j + pc], true);
+    matvec(H, v[j], v[j + pc], false);
     int k0 = 0;
     if (j > pc) {
       k0 = j - pc;
@@ -476,23 +544,35 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
       rec_coef.push_back(T(k, j));
     }
     mops.multiaxpy(rec_vecs, rec_coef, v[j + pc], n, s);
-    for (int idx : I) {
-      double w = red.dot(v[idx], v[j + pc], n, s);
-      axpy(v[j + pc], v[idx], -w, n, s);
-      T(idx, j) = w;
+    for (size_t q = 0; q < I.size(); ++q) {
+      const int slot = j * slots + 1 + (int)q;
+      red.dot_dev(v[I[q]], v[j + pc], n, tdev.p + slot, s);
+      axpy_neg_dev(v[j + pc], v[I[q]], tdev.p + slot, n, s);
+      pend.push_back({slot, I[q], j});  // t(idx, j) = t(j, idx)
     }
-    double w = red.dot(v[j], v[j + pc], n, s);
-    axpy(v[j + pc], v[j], -w, n, s);
-    T(j, j) = w;
-    for (int idx : I) T(j, idx) = T(idx, j);
+    red.dot_dev(v[j], v[j + pc], n, tdev.p + j * slots, s);
+    axpy_neg_dev(v[j + pc], v[j], tdev.p + j * slots, n, s);
+    pend.push_back({j * slots, j, j});
     if (j >= 4 * p && j % p == 0) {
-      std::vector<double> ev;
-      solver.syevd(t, M0, j, false, s, ev, nullptr);
-      double test = std::fabs(ev[0] - ev_old);
-      ev_old = ev[0];
+      flush();
+      // Until a vector deflates inside the band, t is a band matrix of half
+      // bandwidth p, and its lowest eigenvalue comes from banded-Cholesky
+      // bisection on the host; a deflated vector adds entries outside the
+      // band, and then the device eigensolver takes the whole block.
+      double e0;
+      if (I.empty()) {
+        e0 = band_lowest(t, M0, j, p);
+      } else {
+        std::vector<double> ev;
+        solver.syevd(t, M0, j, false, s, ev, nullptr);
+        e0 = ev[0];
+      }
+      double test = std::fabs(e0 - ev_old);
+      ev_old = e0;
       if (test < acc_band) break;
     }
   }
+  flush();
   out.M = j;
   if (j == 0) return out;
   std::vector<double> U;

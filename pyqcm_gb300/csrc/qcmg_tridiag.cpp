@@ -79,4 +79,54 @@ double tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b
   return lam;
 }
 
+// True when A - sigma I is positive definite; A is the leading n x n block
+// of the band matrix, L (n x (b+1), row i holds L(i, i-b..i)) is scratch.
+static bool band_posdef(const std::vector<double>& t, int ld, int n, int b, double sigma,
+                        std::vector<double>& L) {
+  const int w = b + 1;
+  auto Lr = [&](int i, int k) -> double& { return L[(size_t)i * w + (k - i + b)]; };
+  for (int i = 0; i < n; ++i) {
+    const int k0 = std::max(0, i - b);
+    for (int k = k0; k <= i; ++k) {
+      double s = t[(size_t)i + (size_t)ld * k] - (k == i ? sigma : 0.0);
+      for (int m = std::max(k0, k - b); m < k; ++m) s -= Lr(i, m) * Lr(k, m);
+      if (k < i) {
+        Lr(i, k) = s / Lr(k, k);
+      } else {
+        if (!(s > 0.0)) return false;
+        Lr(i, i) = std::sqrt(s);
+      }
+    }
+  }
+  return true;
+}
+
+double band_lowest(const std::vector<double>& t, int ld, int n, int b) {
+  if (n <= 0) return 0.0;
+  b = std::max(0, std::min(b, n - 1));
+  auto A = [&](int r, int c) { return r >= c ? t[(size_t)r + (size_t)ld * c] : t[(size_t)c + (size_t)ld * r]; };
+  // lambda_min <= min_i A(i,i); Gershgorin gives the lower end.
+  double lo = INFINITY, hi = INFINITY, scale = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double r = 0.0;
+    for (int k = std::max(0, i - b); k <= std::min(n - 1, i + b); ++k)
+      if (k != i) r += std::fabs(A(i, k));
+    lo = std::min(lo, A(i, i) - r);
+    hi = std::min(hi, A(i, i));
+    scale = std::max(scale, std::fabs(A(i, i)) + r);
+  }
+  lo -= 4.0 * DBL_EPSILON * std::max(scale, 1.0);
+  std::vector<double> L((size_t)n * (b + 1));
+  // invariant: A - lo I definite, A - hi I not
+  for (int it = 0; it < 2000; ++it) {
+    const double mid = 0.5 * (lo + hi);
+    if (mid <= lo || mid >= hi) break;
+    if (band_posdef(t, ld, n, b, mid, L))
+      lo = mid;
+    else
+      hi = mid;
+  }
+  return 0.5 * (lo + hi);
+}
+
 }  // namespace qcmg

@@ -17,4 +17,16 @@ namespace qcmg {
 double tridiag_lowest(const std::vector<double>& alpha, const std::vector<double>& beta,
                       std::vector<double>& z);
 
+// Lowest eigenvalue of the leading n x n block of a symmetric band matrix
+// (half bandwidth b: t(r, c) = 0 for |r - c| > b), read from the lower
+// triangle of column-major t with leading dimension ld.  Bisection on
+// positive definiteness of t - sigma I, tested by a banded Cholesky
+// factorization (O(n b^2) per probe, no pivoting needed for a definiteness
+// test), so the result is accurate to the factorization's backward error,
+// a few units of eps * ||t||.  This is the convergence probe of band Lanczos
+// (src_ed/Hamiltonian/Lanczos.hpp:338-362 compares the lowest eigenvalue of
+// the projected matrix every p steps); a dense eigensolver per probe costs
+// O(n^3) for the one number it needs.
+double band_lowest(const std::vector<double>& t, int ld, int n, int b);
+
 }  // namespace qcmg

@@ -483,6 +483,27 @@ class ModelInstance:
             S = S + self.hybridization_function(z, spin_down)
         return z * np.eye(len(tc)) - S
 
+    def hybridization_function_many(self, zs, spin_down=False):
+        """Gamma(z) for every z of zs at once: (nz, L, L)."""
+        _, tcb, tb = self.hopping_blocks(spin_down)
+        zs = np.atleast_1d(np.asarray(zs, np.complex128))
+        d = np.diag(tb) if tb.size else np.zeros(0)
+        w = 1.0 / (zs[:, None] - d[None, :])
+        return np.einsum("ik,zk,jk->zij", tcb, w, tcb.conj())
+
+    def self_energy_many(self, zs, spin_down=False):
+        """Sigma(z) for every z of zs at once: one batched Green-function
+        evaluation and one batched inverse instead of a loop over z."""
+        zs = np.atleast_1d(np.asarray(zs, np.complex128))
+        G = self.Green_function(zs, spin_down)
+        if G.ndim == 2:
+            G = G[None]
+        tc, _, _ = self.hopping_blocks(spin_down)
+        S = np.linalg.inv(G) + tc[None]
+        if self.model.n_bath:
+            S = S + self.hybridization_function_many(zs, spin_down)
+        return zs[:, None, None] * np.eye(len(tc))[None] - S
+
     def SEF_bath(self):
         sef = 0.0
         for sd in ((False, True) if self.mixing & 4 else (False,)):

@@ -348,15 +348,13 @@ class LatticeInstance:
         self._host_weights = as_f64(weights)
         self._host = {}
         spins = (False, True) if self.cluster.mixing & 4 else (False,)
+        zs = 1j * self._host_freqs
         for sd in spins:
             P = self.projected_Green_function(self._host_freqs, kside, sd)
             tc, _, _ = self.cluster.hopping_blocks(sd)
-            H = []
-            for i, w in enumerate(self._host_freqs):
-                z = 1j * w
-                X = self.cluster.self_energy(z, sd)
-                H.append(np.linalg.inv(P[i]) + X + tc - z * np.eye(len(tc)))
-            self._host[sd] = np.array(H)
+            X = self.cluster.self_energy_many(zs, sd)
+            eye = np.eye(len(tc))
+            self._host[sd] = np.linalg.inv(P) + X + tc[None] - zs[:, None, None] * eye[None]
         return self._host
 
     def CDMFT_distance(self, bath_values):

@@ -51,6 +51,25 @@ def test_exact_jacobian_against_central_differences(case):
         e[p] = h
         fd = (fit.residuals(x + e) - fit.residuals(x - e)) / (2 * h)
         assert np.max(np.abs(J[:, p] - fd)) <= 1e-7 * max(1.0, np.max(np.abs(fd))), p
+    # the accumulation used when a parameter hits one row twice gives the same
+    fit.theta_unique = fit.E_unique = False
+    assert np.allclose(fit.jacobian(x), J, rtol=0, atol=1e-14 * np.max(np.abs(J)))
+
+
+def test_jacobian_with_a_nondiagonal_bath(case):
+    """A bath-bath hopping makes E non-diagonal: the resolvent then comes
+    from the full inverse; the Jacobian still matches central differences."""
+    fit = _fit(case, ["eb1", "eb2", "tb1", "tb2"])
+    fit.E0 = fit.E0.copy()
+    fit.E0[0, 1] = fit.E0[1, 0] = 0.3
+    x = np.array([-1.0, 1.0, 0.5, 0.4])
+    J = fit.jacobian(x)
+    h = 1e-6
+    for p in range(len(x)):
+        e = np.zeros_like(x)
+        e[p] = h
+        fd = (fit.residuals(x + e) - fit.residuals(x - e)) / (2 * h)
+        assert np.max(np.abs(J[:, p] - fd)) <= 1e-7 * max(1.0, np.max(np.abs(fd))), p
 
 
 def test_fit_lowers_the_distance(case):
