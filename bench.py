@@ -441,7 +441,7 @@ def run_cdmft(args):
     import torch
     from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model
     torch.cuda.set_device(0)
-    nb = args.bath
+    nb = args.bath or 8
     sector = {4: "R0:N8:S0", 8: "R0:N12:S0"}[nb]
     names = bath_names(nb)
     rows = []
@@ -486,7 +486,7 @@ def run_warmstart(args):
     import torch
     from pyqcm_gb300 import warmstart as ws
     torch.cuda.set_device(0)
-    nb = args.bath
+    nb = args.bath or 4
     path = args.warm_data or os.path.join(ROOT, "pyqcm_gb300", "data", f"warmstart_{nb}bath_train.npz")
     P, Y = ws.load(path)
     t0 = time.perf_counter()
@@ -526,8 +526,9 @@ def main():
     ap.add_argument("--workload", default="product",
                     choices=["product", "lanczos", "sef", "cpt", "cdmft", "warmstart"],
                     help="product (the headline line) or one of the secondary measurements")
-    ap.add_argument("--bath", type=int, default=8, choices=[4, 8],
-                    help="bath orbitals of the CDMFT workload")
+    ap.add_argument("--bath", type=int, default=None, choices=[4, 8],
+                    help="bath orbitals (default: 8 for cdmft, 4 for warmstart, whose "
+                         "training set is the 4-bath one)")
     ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
     ap.add_argument("--warm-data", default=None, help="training set of the warm-start workload")
