@@ -96,47 +96,7 @@ __global__ void k_fx_to_f64(const int64_t* __restrict__ q, double* __restrict__ 
     x[i] = c * fx_to_f64(q[i], E);
 }
 
-// Exact dot product sum_i (a_i b_i >> 20), as a 128-bit integer per block.
-__device__ __forceinline__ I128 warp_sum128(I128 v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    I128 w;
-    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
-    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
-    v = add128(v, w);
-  }
-  return v;
-}
-
-__device__ __forceinline__ I128 shr128(I128 v, int s) {  // arithmetic, 0 < s < 64
-  I128 r;
-  r.lo = (v.lo >> s) | ((uint64_t)v.hi << (64 - s));
-  r.hi = v.hi >> s;
-  return r;
-}
-
-constexpr int kDotShift = 20;
 constexpr int kRedBlocksFx = 1024;
-
-__device__ __forceinline__ void block_store128(I128 s, I128* part) {
-  __shared__ int64_t shi[32];
-  __shared__ uint64_t slo[32];
-  s = warp_sum128(s);
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  if (lane == 0) {
-    shi[w] = s.hi;
-    slo[w] = s.lo;
-  }
-  __syncthreads();
-  if (w == 0) {
-    const int nw = (blockDim.x + 31) >> 5;
-    I128 t;
-    t.hi = lane < nw ? shi[lane] : 0;
-    t.lo = lane < nw ? slo[lane] : 0;
-    t = warp_sum128(t);
-    if (lane == 0) part[blockIdx.x] = t;
-  }
-}
 
 // Exact <a, b> partials, two elements per 16-byte load (the fixed-point
 // vectors come from cudaMalloc, so even indices are 16-byte aligned); the
@@ -421,7 +381,8 @@ double FxReducer::dot(const FxVec& a, const FxVec& b, cudaStream_t s) {
 // y = H x  (or y = H x + gamma * yin with yin != nullptr, yin may be &y).
 // The output exponent follows from the bound |H|_inf (T.b) and the input's
 // largest component; c_y = c_x.
-void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma) {
+void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma,
+               FxReducer* dot, double* dot_out) {
   FxTables& T = H->fx;
   cudaStream_t s = H->stream;
   const size_t n = H->dim;
@@ -488,10 +449,29 @@ void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, 
   A.ell4 = T.ell4.p;
   A.cnt4 = T.cnt4.p;
   A.err = T.err.p;
-  launch_product(H, A, s);
+  A.dot_x = nullptr;
+  A.dot_part = nullptr;
+  if (dot) {
+    int sms = 0;
+    QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
+    dot->part.alloc(std::max<size_t>(kRedBlocksFx, product_dot_partials(sms)));
+    dot->out.alloc(1);
+    A.dot_x = x.buf.p;
+    A.dot_part = dot->part.p;
+  }
+  const unsigned np = launch_product(H, A, s);
   y.E = Eo;
   y.mb = kFxBits;
   y.c = x.c;
+  if (dot) {
+    k_fx_final<<<1, 32, 0, s>>>(dot->part.p, (int)np, dot->out.p);
+    QCMG_CUDA(cudaGetLastError());
+    I128 h;
+    QCMG_CUDA(cudaMemcpyAsync(&h, dot->out.p, sizeof(I128), cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+    const double r = std::ldexp((double)h.hi, 64) + (double)h.lo;
+    *dot_out = x.c * y.c * std::ldexp(r, kDotShift + x.E + y.E);
+  }
 }
 
 void fx_check_error(qcmg_hamiltonian* H) {
@@ -602,8 +582,14 @@ LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, 
         QCMG_CUDA(cudaGetLastError());
         if (j + 1 == nsteps) break;
       }
-      fx_matvec(H, *v, *w, nullptr, 0.0);
-      double a = replay ? res.alpha[j] : red.dot(*v, *w, s);
+      // alpha = <v, H v> comes out of the product's second pass
+      double a = 0.0;
+      if (replay) {
+        fx_matvec(H, *v, *w, nullptr, 0.0);
+        a = res.alpha[j];
+      } else {
+        fx_matvec(H, *v, *w, nullptr, 0.0, &red, &a);
+      }
       double n2 = 0.0;
       fx_update(H, *w, *v, have_p ? p : nullptr, a, beta_prev, red, &n2);
       double b = replay ? res.beta[j] : std::sqrt(n2);

@@ -59,6 +59,48 @@ __device__ __forceinline__ int64_t shr128_round(I128 v, int s) {
   return v.hi >> (s - 64);
 }
 
+// Dot products sum_i (a_i b_i >> kDotShift), accumulated as 128-bit integers
+// (order-independent, so any split of the sum gives the same bits).
+__device__ __forceinline__ I128 warp_sum128(I128 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    I128 w;
+    w.hi = __shfl_xor_sync(0xffffffffu, v.hi, o);
+    w.lo = __shfl_xor_sync(0xffffffffu, v.lo, o);
+    v = add128(v, w);
+  }
+  return v;
+}
+
+__device__ __forceinline__ I128 shr128(I128 v, int s) {  // arithmetic, 0 < s < 64
+  I128 r;
+  r.lo = (v.lo >> s) | ((uint64_t)v.hi << (64 - s));
+  r.hi = v.hi >> s;
+  return r;
+}
+
+constexpr int kDotShift = 20;
+
+__device__ __forceinline__ void block_store128(I128 s, I128* part) {
+  __shared__ int64_t shi[32];
+  __shared__ uint64_t slo[32];
+  s = warp_sum128(s);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) {
+    shi[w] = s.hi;
+    slo[w] = s.lo;
+  }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    I128 t;
+    t.hi = lane < nw ? shi[lane] : 0;
+    t.lo = lane < nw ? slo[lane] : 0;
+    t = warp_sum128(t);
+    if (lane == 0) part[blockIdx.x] = t;
+  }
+}
+
 // round(a * m / 2^s)
 __device__ __forceinline__ int64_t mul_fix(int64_t a, int64_t m, int s) {
   return shr128_round(mul_s64(a, m), s);

@@ -23,7 +23,10 @@ bool fx_prepare(qcmg_hamiltonian* H);
 void fx_from_f64(const double* x, size_t n, FxVec& v, cudaStream_t s,
                  DevBuf<unsigned long long>& tmp);
 void fx_to_f64(const FxVec& v, double* x, cudaStream_t s);
-void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma);
+// With dot set, also returns <x, y> for the finished y (computed by the
+// product's second pass, bit-identical to FxReducer::dot(x, y)).
+void fx_matvec(qcmg_hamiltonian* H, const FxVec& x, FxVec& y, const FxVec* yin, double gamma,
+               FxReducer* dot = nullptr, double* dot_out = nullptr);
 // Throws if a kernel of the fast path reported a bounded-wait failure.
 void fx_check_error(qcmg_hamiltonian* H);
 // y (+)= H x on FP64 device vectors through the fixed-point product.

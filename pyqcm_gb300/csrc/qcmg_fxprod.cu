@@ -318,8 +318,10 @@ __device__ __forceinline__ void passD_accum(const int64_t* __restrict__ x, uint3
 }
 
 // VEC = 2 needs du even (every slab segment at an even row is 16-byte
-// aligned); bands start at multiples of 256 rows.
-template <int VEC, bool FAST>
+// aligned); bands start at multiples of 256 rows.  DOT: also the dot
+// product of the finished y with A.dot_x (the element of x at the same
+// place is in the band of x that L2 holds).
+template <int VEC, bool FAST, bool DOT>
 __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
   const uint32_t du = A.du, dd = A.dd;
   const uint32_t lane = threadIdx.x & 31u;
@@ -327,6 +329,7 @@ __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
   const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
   const size_t items = (size_t)A.nbands * dd;
   constexpr uint32_t kSweep = 64u * VEC;  // rows per warp sweep: two VEC-chunks per lane
+  I128 dot = {0, 0};
   for (size_t it = warp; it < items; it += nwarps) {
     const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
     const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
@@ -349,13 +352,22 @@ __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
       auto term = [&](int64_t v) {
         return FAST ? rshift_fixed(v, A.t_dn, A.r_dn) : mul_fix(v, A.mt_dn, A.sh_dn);
       };
-      if (VEC == 2) {
+      const int64_t* xrow = DOT ? A.dot_x + (size_t)a * du : nullptr;
+      auto acc_dot = [&](int64_t yv, int64_t xv) {
+        dot = add128(dot, shr128(mul_s64(yv, xv), kDotShift));
+      };
+      if constexpr (VEC == 2) {
         if (va) {
           longlong2* yp = reinterpret_cast<longlong2*>(yrow + ia);
           longlong2 v = __ldcs(yp);
           v.x += term(P[0] - N[0]);
           v.y += term(P[1] - N[1]);
           __stcs(yp, v);
+          if (DOT) {
+            const longlong2 xv = __ldcg(reinterpret_cast<const longlong2*>(xrow + ia));
+            acc_dot(v.x, xv.x);
+            acc_dot(v.y, xv.y);
+          }
         }
         if (vb) {
           longlong2* yp = reinterpret_cast<longlong2*>(yrow + ib);
@@ -363,13 +375,27 @@ __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
           v.x += term(P[2] - N[2]);
           v.y += term(P[3] - N[3]);
           __stcs(yp, v);
+          if (DOT) {
+            const longlong2 xv = __ldcg(reinterpret_cast<const longlong2*>(xrow + ib));
+            acc_dot(v.x, xv.x);
+            acc_dot(v.y, xv.y);
+          }
         }
       } else {
-        if (va) __stcs(yrow + ia, __ldcs(yrow + ia) + term(P[0] - N[0]));
-        if (vb) __stcs(yrow + ib, __ldcs(yrow + ib) + term(P[1] - N[1]));
+        if (va) {
+          const int64_t v = __ldcs(yrow + ia) + term(P[0] - N[0]);
+          __stcs(yrow + ia, v);
+          if (DOT) acc_dot(v, __ldcg(xrow + ia));
+        }
+        if (vb) {
+          const int64_t v = __ldcs(yrow + ib) + term(P[1] - N[1]);
+          __stcs(yrow + ib, v);
+          if (DOT) acc_dot(v, __ldcg(xrow + ib));
+        }
       }
     }
   }
+  if (DOT) block_store128(dot, A.dot_part);  // every thread of the block gets here
 }
 
 // ---------------------------------------------------------------------------
@@ -519,7 +545,7 @@ static void launch_passU4(Kern kern, const qcmg_hamiltonian* H, const FxProdArgs
   kern<<<(unsigned)grid, threads, smem, s>>>(A);
 }
 
-void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s) {
+unsigned launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s) {
   const FxTables& T = H->fx;
   int sms = 0;
   QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
@@ -563,14 +589,21 @@ void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t
   // pass D
   const size_t items = (size_t)A.nbands * H->dd;
   const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * 8));
+  auto passD = [&](auto vec_tag, auto fast_tag) {
+    constexpr int V = decltype(vec_tag)::value;
+    constexpr bool F = decltype(fast_tag)::value;
+    if (A.dot_part) k_fx_passD4<V, F, true><<<gD, 256, 0, s>>>(A);
+    else k_fx_passD4<V, F, false><<<gD, 256, 0, s>>>(A);
+  };
   if ((H->du & 1u) == 0u) {
-    if (fast) k_fx_passD4<2, true><<<gD, 256, 0, s>>>(A);
-    else k_fx_passD4<2, false><<<gD, 256, 0, s>>>(A);
+    if (fast) passD(Two{}, Fast{});
+    else passD(Two{}, Full{});
   } else {
-    if (fast) k_fx_passD4<1, true><<<gD, 256, 0, s>>>(A);
-    else k_fx_passD4<1, false><<<gD, 256, 0, s>>>(A);
+    if (fast) passD(One{}, Fast{});
+    else passD(One{}, Full{});
   }
   QCMG_CUDA(cudaGetLastError());
+  return gD;
 }
 
 }  // namespace qcmg

@@ -8,6 +8,8 @@
 
 namespace qcmg {
 
+struct I128;
+
 struct FxProdArgs {
   uint32_t du, dd;
   int L;
@@ -52,6 +54,10 @@ struct FxProdArgs {
   const uint2* ell4;
   const uint16_t* cnt4;
   int* err;  // set to 1 when a bounded wait gives up
+  // optional: pass D also accumulates sum_i (y_i dot_x_i >> kDotShift), one
+  // 128-bit partial per pass-D block into dot_part (the Lanczos alpha)
+  const int64_t* dot_x;
+  I128* dot_part;
 };
 
 // Builds the grouped ELL form of the up-spin hops from the unit-magnitude
@@ -67,7 +73,11 @@ int choose_slabs_per_pass(uint32_t du, int max_optin_smem);
 // log2 |m| when |m| is a power of two, else -1 (for FxProdArgs::p2_*).
 int pow2_exponent(int64_t m);
 
-// Launches pass U then pass D for y (+)= H x.
-void launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s);
+// Launches pass U then pass D for y (+)= H x; returns pass D's block count
+// (the number of dot partials when A.dot_part is set).
+unsigned launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStream_t s);
+
+// Upper bound of launch_product's return value on a device with sms SMs.
+inline unsigned product_dot_partials(int sms) { return (unsigned)sms * 8u; }
 
 }  // namespace qcmg
