@@ -575,16 +575,25 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   flush();
   out.M = j;
   if (j == 0) return out;
-  std::vector<double> U;
-  solver.syevd(t, M0, j, true, s, out.evals, &U);
   // Q = P(:, 0:k) U(0:k, :), k = min(p, M) (Hamiltonian_base.hpp:249 with
-  // matrix::product's bound on the inner index).
+  // matrix::product's bound on the inner index): all eigenvalues of t but
+  // only the leading k rows of its eigenvectors.  Without in-band
+  // deflation t is a band matrix and the host band solver gives exactly
+  // that; otherwise the device eigensolver takes the whole block.
   const int M = j, kk = std::min(p, M);
+  std::vector<double> U;  // U(k, c) = U[k * ustride_k + c * ustride_c]
+  size_t ustride_k = 1, ustride_c = (size_t)M;
+  if (!(I.empty() && band_eigen_leading(t, M0, M, p, kk, out.evals, U))) {
+    solver.syevd(t, M0, j, true, s, out.evals, &U);
+  } else {
+    ustride_k = (size_t)M;
+    ustride_c = 1;
+  }
   out.Q.assign((size_t)p * M, 0.0);
   for (int a = 0; a < p; ++a)
     for (int c = 0; c < M; ++c) {
       double acc = 0.0;
-      for (int k = 0; k < kk; ++k) acc += P[a + (size_t)p * k] * U[k + (size_t)M * c];
+      for (int k = 0; k < kk; ++k) acc += P[a + (size_t)p * k] * U[k * ustride_k + c * ustride_c];
       out.Q[(size_t)a * M + c] = acc;
     }
   return out;

@@ -129,4 +129,142 @@ double band_lowest(const std::vector<double>& t, int ld, int n, int b) {
   return 0.5 * (lo + hi);
 }
 
+namespace {
+
+// c, s with c a + s b = hypot(a, b) and -s a + c b = 0.
+inline void givens(double a, double b, double* c, double* s) {
+  const double h = std::hypot(a, b);
+  if (h == 0.0) {
+    *c = 1.0;
+    *s = 0.0;
+  } else {
+    *c = a / h;
+    *s = b / h;
+  }
+}
+
+}  // namespace
+
+bool band_eigen_leading(const std::vector<double>& t, int ld, int n, int b, int p,
+                        std::vector<double>& evals, std::vector<double>& W) {
+  evals.assign(std::max(n, 0), 0.0);
+  W.assign((size_t)std::max(p, 0) * std::max(n, 0), 0.0);
+  if (n <= 0 || p <= 0) return true;
+  b = std::max(0, std::min(b, n - 1));
+  // Dense symmetric copy (row-major); the band reduction only touches a
+  // window of width O(b) around each rotation, so the work is O(n^2 b).
+  std::vector<double> A((size_t)n * n, 0.0);
+  for (int c = 0; c < n; ++c)
+    for (int r = c; r <= std::min(n - 1, c + b); ++r) {
+      const double v = t[(size_t)r + (size_t)ld * c];
+      A[(size_t)r * n + c] = v;
+      A[(size_t)c * n + r] = v;
+    }
+  // Z: the leading p rows of the accumulated orthogonal transform, p x n.
+  std::vector<double> Z((size_t)p * n, 0.0);
+  for (int k = 0; k < std::min(p, n); ++k) Z[(size_t)k * n + k] = 1.0;
+  // A <- G A G^T, G the rotation [c s; -s c] on rows/columns (r, r+1);
+  // Z <- Z G^T keeps A_original = Z_full A Z_full^T.
+  auto rotate = [&](int r, double c, double s) {
+    const int lo = std::max(0, r - b - 2), hi = std::min(n, r + b + 4);
+    double* a0 = &A[(size_t)r * n];
+    double* a1 = &A[(size_t)(r + 1) * n];
+    for (int j = lo; j < hi; ++j) {
+      const double x = a0[j], y = a1[j];
+      a0[j] = c * x + s * y;
+      a1[j] = -s * x + c * y;
+    }
+    for (int j = lo; j < hi; ++j) {
+      double* row = &A[(size_t)j * n];
+      const double x = row[r], y = row[r + 1];
+      row[r] = c * x + s * y;
+      row[r + 1] = -s * x + c * y;
+    }
+    for (int k = 0; k < p; ++k) {
+      double* z = &Z[(size_t)k * n];
+      const double x = z[r], y = z[r + 1];
+      z[r] = c * x + s * y;
+      z[r + 1] = -s * x + c * y;
+    }
+  };
+  // Band to tridiagonal (Schwarz's Givens scheme): clear column k below the
+  // subdiagonal from the bottom of the band up; each rotation in the plane
+  // (i-1, i) leaves one element at (i+b, i-1) outside the band, which is
+  // chased down the matrix b rows at a time.
+  for (int k = 0; k + 2 < n; ++k) {
+    for (int i = std::min(k + b, n - 1); i >= k + 2; --i) {
+      if (A[(size_t)i * n + k] == 0.0) continue;
+      double c, s;
+      givens(A[(size_t)(i - 1) * n + k], A[(size_t)i * n + k], &c, &s);
+      rotate(i - 1, c, s);
+      A[(size_t)i * n + k] = A[(size_t)k * n + i] = 0.0;
+      for (int j = i + b; j < n; j += b) {
+        const int col = j - b - 1;
+        if (A[(size_t)j * n + col] == 0.0) break;
+        givens(A[(size_t)(j - 1) * n + col], A[(size_t)j * n + col], &c, &s);
+        rotate(j - 1, c, s);
+        A[(size_t)j * n + col] = A[(size_t)col * n + j] = 0.0;
+      }
+    }
+  }
+  std::vector<double> d(n), e(n, 0.0);
+  for (int i = 0; i < n; ++i) d[i] = A[(size_t)i * n + i];
+  for (int i = 0; i + 1 < n; ++i) e[i] = A[(size_t)(i + 1) * n + i];
+  // Tridiagonal eigenproblem by the implicit QL method with Wilkinson-type
+  // shifts (Bowdler, Martin, Reinsch and Wilkinson, 1968), each plane
+  // rotation also applied to the columns of Z.
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0;; ++iter) {
+      int m = l;
+      for (; m + 1 < n; ++m) {
+        const double dd = std::fabs(d[m]) + std::fabs(d[m + 1]);
+        if (std::fabs(e[m]) <= DBL_EPSILON * dd) break;
+      }
+      if (m == l) break;
+      if (iter == 100) return false;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + std::copysign(r, g));
+      double s = 1.0, c = 1.0, shift = 0.0;
+      bool split = false;
+      for (int i = m - 1; i >= l; --i) {
+        const double f = s * e[i], bb = c * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {  // the subdiagonal underflowed: the matrix splits here
+          d[i + 1] -= shift;
+          e[m] = 0.0;
+          split = true;
+          break;
+        }
+        s = f / r;
+        c = g / r;
+        g = d[i + 1] - shift;
+        r = (d[i] - g) * s + 2.0 * c * bb;
+        shift = s * r;
+        d[i + 1] = g + shift;
+        g = c * r - bb;
+        for (int k = 0; k < p; ++k) {
+          double* z = &Z[(size_t)k * n];
+          const double zf = z[i + 1];
+          z[i + 1] = s * z[i] + c * zf;
+          z[i] = c * z[i] - s * zf;
+        }
+      }
+      if (split) continue;
+      d[l] -= shift;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int c) { return d[a] < d[c]; });
+  for (int i = 0; i < n; ++i) {
+    evals[i] = d[order[i]];
+    for (int k = 0; k < p; ++k) W[(size_t)k * n + i] = Z[(size_t)k * n + order[i]];
+  }
+  return true;
+}
+
 }  // namespace qcmg

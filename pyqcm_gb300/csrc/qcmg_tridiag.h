@@ -29,4 +29,14 @@ double tridiag_lowest(const std::vector<double>& alpha, const std::vector<double
 // O(n^3) for the one number it needs.
 double band_lowest(const std::vector<double>& t, int ld, int n, int b);
 
+// All eigenvalues (ascending) of the same band matrix, and the leading p
+// rows of its eigenvectors: W[k * n + c] is component k of eigenvector c.
+// Band Lanczos needs no more to form its Q-matrix (Q = P U(0:p, :),
+// src_ed/Hamiltonian/Hamiltonian_base.hpp:249), so the full eigenvector
+// matrix is never built: a Givens reduction to tridiagonal form (O(n^2 b))
+// and implicit QL iterations, with every rotation applied to p rows only.
+// False if the QL iteration does not converge.
+bool band_eigen_leading(const std::vector<double>& t, int ld, int n, int b, int p,
+                        std::vector<double>& evals, std::vector<double>& W);
+
 }  // namespace qcmg
