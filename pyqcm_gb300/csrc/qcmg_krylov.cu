@@ -107,6 +107,65 @@ __global__ void __launch_bounds__(256) k_scale_sub(double* __restrict__ v, doubl
   }
 }
 
+// Fixed-order block sum; the result is valid in thread 0.
+__device__ __forceinline__ double block_sum_fixed(double v) {
+  __shared__ double ws[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) ws[w] = v;
+  __syncthreads();
+  v = (threadIdx.x < (blockDim.x >> 5)) ? ws[threadIdx.x] : 0.0;
+  if (w == 0) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  return v;
+}
+
+// w -= sum_k c_k V_k (the band recurrence), then one partial of w . u per
+// block for the closing Gram-Schmidt step against u = v_j.
+template <class VL, class CL>
+__global__ void __launch_bounds__(256) k_multiaxpy_dot(VL V, int m, CL c, double* __restrict__ w,
+                                                       const double* __restrict__ u, size_t n,
+                                                       double* __restrict__ part) {
+  extern __shared__ double cs[];
+  for (int k = threadIdx.x; k < m; k += blockDim.x) cs[k] = c[k];
+  __syncthreads();
+  double d = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double s = w[i];
+    for (int k = 0; k < m; ++k) s = fma(-cs[k], V[k][i], s);
+    w[i] = s;
+    d = fma(s, u[i], d);
+  }
+  d = block_sum_fixed(d);
+  if (threadIdx.x == 0) part[blockIdx.x] = d;
+}
+
+// Every block sums the nb partials in the same fixed order (so all agree on
+// the dot), then w -= dot * u; block 0 also stores the dot at dot_out.
+__global__ void __launch_bounds__(256) k_dot_axpy(const double* __restrict__ part, int nb,
+                                                  const double* __restrict__ u,
+                                                  double* __restrict__ w, size_t n,
+                                                  double* __restrict__ dot_out) {
+  __shared__ double total;
+  double t = 0.0;
+  for (int b = threadIdx.x; b < nb; b += blockDim.x) t += part[b];
+  t = block_sum_fixed(t);
+  if (threadIdx.x == 0) {
+    total = t;
+    if (blockIdx.x == 0) *dot_out = t;
+  }
+  __syncthreads();
+  const double cdot = -total;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    w[i] = fma(cdot, u[i], w[i]);
+}
+
 // Block count of a multi-dot over n elements (fixed: deterministic order).
 int multidot_blocks(size_t n) {
   return (int)std::max<size_t>(1, std::min<size_t>((n + kTile - 1) / kTile, 2 * 152));
@@ -146,10 +205,39 @@ struct MultiOps {
       k_multidot<const double* const*>
           <<<nblocks, 256, m * sizeof(double), s>>>(ptrs.p, m, w, n, part.p);
     }
-    k_multidot_final<<<(m + 127) / 128, 128, 0, s>>>(part.p, nblocks, m, coef.p);
     QCMG_CUDA(cudaGetLastError());
-    QCMG_CUDA(cudaMemcpyAsync(out.data(), coef.p, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    // the partials come back and are summed here in k_multidot_final's order
+    // (one launch fewer per call; the sums are bitwise the same)
+    host.resize((size_t)nblocks * m);
+    QCMG_CUDA(cudaMemcpyAsync(host.data(), part.p, host.size() * sizeof(double),
+                              cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
+    for (int k = 0; k < m; ++k) {
+      double acc = 0.0;
+      for (int b = 0; b < nblocks; ++b) acc += host[(size_t)b * m + k];
+      out[k] = acc;
+    }
+  }
+  // w -= sum_k c_k V_k, then d = w . u and w -= d u with d left at d_dev:
+  // two launches.  False (nothing done) for lists longer than kByValue.
+  DevBuf<double> opart;
+  bool multiaxpy_orth(const std::vector<const double*>& V, const std::vector<double>& c,
+                      double* w, const double* u, size_t n, double* d_dev, cudaStream_t s) {
+    const int m = (int)V.size();
+    if (m > kByValue || n == 0) return false;
+    VecList L;
+    CoefList C;
+    for (int k = 0; k < m; ++k) {
+      L.v[k] = V[k];
+      C.c[k] = c[k];
+    }
+    const unsigned g = elementwise_grid(n);
+    opart.alloc(g);
+    k_multiaxpy_dot<VecList, CoefList>
+        <<<g, 256, std::max(m, 1) * sizeof(double), s>>>(L, m, C, w, u, n, opart.p);
+    k_dot_axpy<<<g, 256, 0, s>>>(opart.p, (int)g, u, w, n, d_dev);
+    QCMG_CUDA(cudaGetLastError());
+    return true;
   }
   static unsigned elementwise_grid(size_t n) {
     return (unsigned)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 152 * 8));
@@ -543,15 +631,20 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
       rec_vecs.push_back(v[k]);
       rec_coef.push_back(T(k, j));
     }
-    mops.multiaxpy(rec_vecs, rec_coef, v[j + pc], n, s);
-    for (size_t q = 0; q < I.size(); ++q) {
-      const int slot = j * slots + 1 + (int)q;
-      red.dot_dev(v[I[q]], v[j + pc], n, tdev.p + slot, s);
-      axpy_neg_dev(v[j + pc], v[I[q]], tdev.p + slot, n, s);
-      pend.push_back({slot, I[q], j});  // t(idx, j) = t(j, idx)
+    // with no deflated vectors the recurrence and the closing step against
+    // v_j are one fused pair of launches
+    if (!(I.empty() &&
+          mops.multiaxpy_orth(rec_vecs, rec_coef, v[j + pc], v[j], n, tdev.p + j * slots, s))) {
+      mops.multiaxpy(rec_vecs, rec_coef, v[j + pc], n, s);
+      for (size_t q = 0; q < I.size(); ++q) {
+        const int slot = j * slots + 1 + (int)q;
+        red.dot_dev(v[I[q]], v[j + pc], n, tdev.p + slot, s);
+        axpy_neg_dev(v[j + pc], v[I[q]], tdev.p + slot, n, s);
+        pend.push_back({slot, I[q], j});  // t(idx, j) = t(j, idx)
+      }
+      red.dot_dev(v[j], v[j + pc], n, tdev.p + j * slots, s);
+      axpy_neg_dev(v[j + pc], v[j], tdev.p + j * slots, n, s);
     }
-    red.dot_dev(v[j], v[j + pc], n, tdev.p + j * slots, s);
-    axpy_neg_dev(v[j + pc], v[j], tdev.p + j * slots, n, s);
     pend.push_back({j * slots, j, j});
     if (j >= 4 * p && j % p == 0) {
       flush();
