@@ -548,6 +548,7 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   std::vector<double> tmp;
   Cusolver solver;
   double ev_old = 1e12;
+  double last_change = INFINITY;
   int j;
   std::vector<const double*> tg;
   std::vector<double*> gs_vecs;
@@ -583,10 +584,15 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
     // One multi-dot on the unscaled v_j gives its norm, its projections on
     // the p start vectors and its dots with the next pc-1 vectors (each of
     // those vectors is changed only by its own update below, so the dots
-    // are independent): one synchronization instead of pc + 1.
+    // are independent): one synchronization instead of pc + 1.  The
+    // projections P(:, j) are taken for j < p only: the Q-matrix product
+    // bounds its inner index by p (Hamiltonian_base.hpp:249), so no later
+    // column of P reaches the result, and on GB300 each dot is an FP64 FMA
+    // per element.
+    const int nproj = j < p ? p : 0;
     tg.clear();
     tg.push_back(v[j]);
-    for (int k = 0; k < p; ++k) tg.push_back(phip[k]);
+    for (int k = 0; k < nproj; ++k) tg.push_back(phip[k]);
     for (int k = j + 1; k < j + pc; ++k) tg.push_back(v[k]);
     mops.multidot(tg, v[j], n, s, tmp);
     double z = std::sqrt(tmp[0]);
@@ -606,11 +612,11 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
     // v_j /= z; v_k -= <v_j, v_k> v_j for the next pc-1 vectors (one kernel)
     const double iz = 1.0 / z;
     if (j >= pc) T(j, j - pc) = z;
-    for (int k = 0; k < p; ++k) P[k + (size_t)p * j] = tmp[1 + k] * iz;
+    for (int k = 0; k < nproj; ++k) P[k + (size_t)p * j] = tmp[1 + k] * iz;
     gs_vecs.clear();
     gs_coef.clear();
     for (int k = j + 1; k < j + pc; ++k) {
-      const double zz = tmp[1 + p + (k - j - 1)] * iz;
+      const double zz = tmp[1 + nproj + (k - j - 1)] * iz;
       gs_vecs.push_back(v[k]);
       gs_coef.push_back(zz);
       if (k >= pc) T(j, k - pc) = zz;
@@ -654,13 +660,22 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
       // band, and then the device eigensolver takes the whole block.
       double e0;
       if (I.empty()) {
-        e0 = band_lowest(t, M0, j, p);
+        // the previous probe's value bounds this one from above (the
+        // earlier block is a leading principal submatrix) and its last
+        // change sizes the starting bracket
+        const bool warm = ev_old < 1e12;
+        const double width =
+            std::isfinite(last_change) && warm
+                ? std::max(4.0 * last_change, 1e-12 * std::max(1.0, std::fabs(ev_old)))
+                : 1e-3 * std::max(1.0, std::fabs(ev_old));
+        e0 = warm ? band_lowest(t, M0, j, p, ev_old, width) : band_lowest(t, M0, j, p);
       } else {
         std::vector<double> ev;
         solver.syevd(t, M0, j, false, s, ev, nullptr);
         e0 = ev[0];
       }
       double test = std::fabs(e0 - ev_old);
+      if (ev_old < 1e12) last_change = test;
       ev_old = e0;
       if (test < acc_band) break;
     }

@@ -101,24 +101,96 @@ static bool band_posdef(const std::vector<double>& t, int ld, int n, int b, doub
   return true;
 }
 
-double band_lowest(const std::vector<double>& t, int ld, int n, int b) {
+// Inverse iteration with the Cholesky factor L of A - sigma I (sigma below
+// the lowest eigenvalue), then the Rayleigh quotient of the iterate: the
+// lowest eigenvalue when the iteration has converged.  O(n b) per step.
+static bool band_refine(const std::vector<double>& t, int ld, int n, int b,
+                        const std::vector<double>& L, double* lam) {
+  const int w = b + 1;
+  auto Lr = [&](int i, int k) { return L[(size_t)i * w + (k - i + b)]; };
+  auto A = [&](int r, int c) {
+    return r >= c ? t[(size_t)r + (size_t)ld * c] : t[(size_t)c + (size_t)ld * r];
+  };
+  std::vector<double> x(n), y(n);
+  for (int i = 0; i < n; ++i) x[i] = 1.0 + 0.25 * std::sin(0.7 * i + 0.3);
+  for (int it = 0; it < 8; ++it) {
+    for (int i = 0; i < n; ++i) {  // L y = x
+      double v = x[i];
+      for (int k = std::max(0, i - b); k < i; ++k) v -= Lr(i, k) * y[k];
+      y[i] = v / Lr(i, i);
+    }
+    for (int i = n - 1; i >= 0; --i) {  // L^T x = y
+      double v = y[i];
+      for (int m = i + 1; m <= std::min(n - 1, i + b); ++m) v -= Lr(m, i) * x[m];
+      x[i] = v / Lr(i, i);
+    }
+    double nrm = 0.0;
+    for (double v : x) nrm += v * v;
+    nrm = std::sqrt(nrm);
+    if (!(nrm > 0.0) || !std::isfinite(nrm)) return false;
+    for (double& v : x) v /= nrm;
+  }
+  double q = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double ax = 0.0;
+    for (int k = std::max(0, i - b); k <= std::min(n - 1, i + b); ++k) ax += A(i, k) * x[k];
+    q += x[i] * ax;
+  }
+  *lam = q;
+  return std::isfinite(q);
+}
+
+double band_lowest(const std::vector<double>& t, int ld, int n, int b, double near,
+                   double width) {
   if (n <= 0) return 0.0;
   b = std::max(0, std::min(b, n - 1));
   auto A = [&](int r, int c) { return r >= c ? t[(size_t)r + (size_t)ld * c] : t[(size_t)c + (size_t)ld * r]; };
   // lambda_min <= min_i A(i,i); Gershgorin gives the lower end.
-  double lo = INFINITY, hi = INFINITY, scale = 0.0;
+  double glo = INFINITY, hi = INFINITY, scale = 0.0;
   for (int i = 0; i < n; ++i) {
     double r = 0.0;
     for (int k = std::max(0, i - b); k <= std::min(n - 1, i + b); ++k)
       if (k != i) r += std::fabs(A(i, k));
-    lo = std::min(lo, A(i, i) - r);
+    glo = std::min(glo, A(i, i) - r);
     hi = std::min(hi, A(i, i));
     scale = std::max(scale, std::fabs(A(i, i)) + r);
   }
-  lo -= 4.0 * DBL_EPSILON * std::max(scale, 1.0);
+  glo -= 4.0 * DBL_EPSILON * std::max(scale, 1.0);
   std::vector<double> L((size_t)n * (b + 1));
-  // invariant: A - lo I definite, A - hi I not
+  double lo = glo;
+  if (std::isfinite(near) && std::isfinite(width) && width > 0.0) {
+    // start from a bracket below the hint and widen it until A - lo I is
+    // definite (the Gershgorin end always is)
+    const double top = near + 64.0 * DBL_EPSILON * std::max(scale, 1.0);
+    if (top < hi && !band_posdef(t, ld, n, b, top, L)) hi = top;
+    for (double w = width;; w *= 8.0) {
+      const double cand = hi - w;
+      if (cand <= glo) break;
+      if (band_posdef(t, ld, n, b, cand, L)) {
+        lo = cand;
+        break;
+      }
+      hi = cand;
+    }
+  }
+  // invariant: A - lo I definite, A - hi I not.  Bisect to a bracket of
+  // 1e-4 of the matrix scale, then refine by inverse iteration with the
+  // definite shift lo and a Rayleigh quotient; the refined value is taken
+  // only if two definiteness probes confirm it to eta (else bisection runs
+  // on to full precision), so it is as reliable as bisection.
+  const double refine_at = 1e-4 * std::max(scale, 1.0);
+  const double eta = 16.0 * DBL_EPSILON * std::max(scale, 1.0);
+  bool tried = false;
   for (int it = 0; it < 2000; ++it) {
+    if (!tried && hi - lo <= refine_at) {
+      tried = true;
+      double lam;
+      if (band_posdef(t, ld, n, b, lo, L) && band_refine(t, ld, n, b, L, &lam) &&
+          lam - eta > lo && lam + eta < hi) {
+        if (band_posdef(t, ld, n, b, lam - eta, L) && !band_posdef(t, ld, n, b, lam + eta, L))
+          return lam;
+      }
+    }
     const double mid = 0.5 * (lo + hi);
     if (mid <= lo || mid >= hi) break;
     if (band_posdef(t, ld, n, b, mid, L))

@@ -8,6 +8,7 @@
 // with an LDL^T factorization, O(n) per solve).
 #pragma once
 
+#include <cmath>
 #include <vector>
 
 namespace qcmg {
@@ -26,8 +27,13 @@ double tridiag_lowest(const std::vector<double>& alpha, const std::vector<double
 // a few units of eps * ||t||.  This is the convergence probe of band Lanczos
 // (src_ed/Hamiltonian/Lanczos.hpp:338-362 compares the lowest eigenvalue of
 // the projected matrix every p steps); a dense eigensolver per probe costs
-// O(n^3) for the one number it needs.
-double band_lowest(const std::vector<double>& t, int ld, int n, int b);
+// O(n^3) for the one number it needs.  A hint (near, width > 0: the
+// lowest eigenvalue is expected just below near, within about width; the
+// previous probe's value and change) narrows the starting bracket, which
+// then widens geometrically until it holds the eigenvalue, so a wrong hint
+// costs probes, not accuracy.
+double band_lowest(const std::vector<double>& t, int ld, int n, int b, double near = NAN,
+                   double width = 0.0);
 
 // All eigenvalues (ascending) of the same band matrix, and the leading p
 // rows of its eigenvectors: W[k * n + c] is component k of eigenvector c.

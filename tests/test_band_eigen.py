@@ -30,8 +30,12 @@ int main() {
     for (double& v : t) std::scanf("%lf", &v);
     std::vector<double> ev, W;
     const double lo = qcmg::band_lowest(t, ld, n, b);
+    // hinted: from just above, and from a wrong hint far above and below
+    const double lo_near = qcmg::band_lowest(t, ld, n, b, lo + 1e-9, 1e-6);
+    const double lo_high = qcmg::band_lowest(t, ld, n, b, lo + 3.0, 1e-9);
+    const double lo_low = qcmg::band_lowest(t, ld, n, b, lo - 3.0, 1e-9);
     const bool ok = qcmg::band_eigen_leading(t, ld, n, b, p, ev, W);
-    std::printf("%d %.17g\n", ok ? 1 : 0, lo);
+    std::printf("%d %.17g %.17g %.17g %.17g\n", ok ? 1 : 0, lo, lo_near, lo_high, lo_low);
     for (double v : ev) std::printf("%.17g\n", v);
     for (double v : W) std::printf("%.17g\n", v);
   }
@@ -82,8 +86,8 @@ def _run(driver, mats):
     res, o = [], 0
     for A, b, p in mats:
         n = A.shape[0]
-        ok, lo = int(out[o]), float(out[o + 1])
-        o += 2
+        ok, lo = int(out[o]), np.array(out[o + 1:o + 5], float)
+        o += 5
         ev = np.array(out[o:o + n], float)
         o += n
         W = np.array(out[o:o + p * n], float).reshape(p, n)
@@ -103,12 +107,18 @@ def test_band_solvers_against_numpy(driver):
         mats.append((_band(rng, n, b), b, p))
     # a repeated diagonal gives near-degenerate clusters
     mats.append((_band(rng, 60, 2, diag=(np.arange(60) % 3) - 1.0), 2, 4))
+    # an exactly degenerate lowest eigenvalue (two uncoupled copies of one block)
+    B = _band(rng, 30, 3)
+    D = np.zeros((60, 60))
+    D[::2, ::2] = B
+    D[1::2, 1::2] = B
+    mats.append((D, 7, 4))
     for (A, b, p), (ok, lo, ev, W) in zip(mats, _run(driver, mats)):
         n = A.shape[0]
         w, V = np.linalg.eigh(A)
         scale = np.abs(A).max()
         assert ok
-        assert abs(lo - w[0]) <= 1e-13 * scale, (n, b)
+        assert np.max(np.abs(lo - w[0])) <= 1e-13 * scale, (n, b, lo - w[0])
         assert np.max(np.abs(ev - w)) <= 1e-13 * scale, (n, b)
         k = min(p, n)
         assert np.max(np.abs(W[:k] @ W[:k].T - np.eye(k))) < 1e-13
