@@ -193,6 +193,16 @@ int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_targe
                       double acc_deflation, double acc_band, int* M, double* evals, double* Q,
                       int cap);
 
+/* qcmg_band_lanczos with the start vectors already in the handle's device
+ * memory (p x dim, row-major; e.g. written there by qcmg_apply_c with
+ * QCMG_DEVICE_PTRS), so they cross no host link.  The call waits for the
+ * device before reading them and only reads them.  Same reference
+ * interface as qcmg_band_lanczos (Hamiltonian_base.hpp:229-254), whose
+ * start vectors the reference builds in host memory. */
+int qcmg_band_lanczos_device(qcmg_hamiltonian* H, int p, const double* phi_dev, int M_target,
+                             int max_iter, double acc_deflation, double acc_band, int* M,
+                             double* evals, double* Q, int cap);
+
 /* c_orb (pm = -1) or c^dagger_orb (pm = +1) applied to x of sector
  * (n_up, n_dn) on L orbitals; orb >= L is a down orbital.  y (target sector,
  * length dim_up' * dim_dn') receives y (+)= z * c x.

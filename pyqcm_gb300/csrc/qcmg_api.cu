@@ -447,9 +447,9 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
   });
 }
 
-int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_target, int max_iter,
-                      double acc_deflation, double acc_band, int* M, double* evals, double* Q,
-                      int cap) {
+static int band_lanczos_entry(qcmg_hamiltonian* H, int p, const double* phi, bool on_device,
+                              int M_target, int max_iter, double acc_deflation, double acc_band,
+                              int* M, double* evals, double* Q, int cap) {
   return guarded([&] {
     QCMG_CHECK_ARG(H != nullptr && phi != nullptr && M != nullptr, "NULL argument");
     QCMG_CHECK_ARG(p > 0 && M_target > 1 && max_iter > 0, "invalid band Lanczos sizes");
@@ -457,12 +457,28 @@ int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_targe
     QCMG_CUDA(cudaSetDevice(H->device));
     *M = 0;
     if (H->dim == 0) return;
-    BandResult r = band_lanczos(H, p, phi, M_target, max_iter, acc_deflation, acc_band);
+    // device start vectors may come from any stream: wait for the device
+    if (on_device) QCMG_CUDA(cudaDeviceSynchronize());
+    BandResult r = band_lanczos(H, p, phi, on_device, M_target, max_iter, acc_deflation, acc_band);
     *M = r.M;
     QCMG_CHECK_ARG(r.M <= cap, "band Lanczos output capacity too small");
     if (evals) std::copy(r.evals.begin(), r.evals.end(), evals);
     if (Q) std::copy(r.Q.begin(), r.Q.end(), Q);
   });
+}
+
+int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_target, int max_iter,
+                      double acc_deflation, double acc_band, int* M, double* evals, double* Q,
+                      int cap) {
+  return band_lanczos_entry(H, p, phi, false, M_target, max_iter, acc_deflation, acc_band, M,
+                            evals, Q, cap);
+}
+
+int qcmg_band_lanczos_device(qcmg_hamiltonian* H, int p, const double* phi_dev, int M_target,
+                             int max_iter, double acc_deflation, double acc_band, int* M,
+                             double* evals, double* Q, int cap) {
+  return band_lanczos_entry(H, p, phi_dev, true, M_target, max_iter, acc_deflation, acc_band, M,
+                            evals, Q, cap);
 }
 
 int qcmg_apply_c(int L, int orb, int pm, int n_up, int n_dn, const double* x, double* y, double z,

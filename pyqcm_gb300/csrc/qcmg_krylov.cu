@@ -498,7 +498,8 @@ struct Cusolver {
   }
 };
 
-BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int M0, int max_iter,
+BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device, int M0,
+                        int max_iter,
                         double acc_defl, double acc_band) {
   const size_t n = H->dim;
   cudaStream_t s = H->stream;
@@ -509,13 +510,17 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   int M0p = (M0 / p + 1) * p;
   M0 = M0p - pc;
   QCMG_CHECK_ARG(M0 > 0, "band Lanczos needs M > 0");
-  // Device vectors: the p start vectors plus a pool for v[0..M0p).
+  // Device vectors: the p start vectors (the caller's own when they are on
+  // the device: they are only read) plus a pool for v[0..M0p).
   std::vector<DevVec> phi;
   std::vector<const double*> phip;
   for (int k = 0; k < p; ++k) {
+    if (phi_on_device) {
+      phip.push_back(phi_in + (size_t)k * n);
+      continue;
+    }
     phi.emplace_back(n);
-    QCMG_CUDA(cudaMemcpyAsync(phi[k].p, phi_host + (size_t)k * n, n * 8, cudaMemcpyHostToDevice,
-                              s));
+    QCMG_CUDA(cudaMemcpyAsync(phi[k].p, phi_in + (size_t)k * n, n * 8, cudaMemcpyHostToDevice, s));
     phip.push_back(phi[k].p);
   }
   std::vector<double*> v(M0p, nullptr);
@@ -536,7 +541,7 @@ BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int 
   };
   for (int i = 0; i < p; ++i) {
     v[i] = get();
-    QCMG_CUDA(cudaMemcpyAsync(v[i], phi[i].p, n * 8, cudaMemcpyDeviceToDevice, s));
+    QCMG_CUDA(cudaMemcpyAsync(v[i], phip[i], n * 8, cudaMemcpyDeviceToDevice, s));
   }
   std::vector<double> t((size_t)M0 * M0, 0.0);  // column-major t(r,c) = t[r + M0*c]
   auto T = [&](int r, int c) -> double& { return t[(size_t)r + (size_t)M0 * c]; };

@@ -28,8 +28,10 @@ void seeded_vector(size_t dim, unsigned seed, double* out);
 LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,
                                    double tol, int max_iter, int reorth, double* psi_host);
 
-BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_host, int M0, int max_iter,
-                        double acc_defl, double acc_band);
+// phi_in: p start vectors of length dim, vector k at phi_in + k*dim, in
+// host memory or (phi_on_device) in the handle's device memory.
+BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device,
+                        int M0, int max_iter, double acc_defl, double acc_band);
 
 void launch_apply_c(int L, int orb, int spin, int pm, int nup, int ndn, const double* x, double* y,
                     double z, bool accumulate, cudaStream_t s);

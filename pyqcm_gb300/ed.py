@@ -253,13 +253,27 @@ class Hamiltonian:
         if M <= 1:
             M = 2
         phis = np.ascontiguousarray(np.array(phi, np.float64).reshape(p, self.dim))
+        return self._band_lanczos(p, ptr(phis), M, lib().qcmg_band_lanczos)
+
+    def build_Q_matrix_device(self, phi_dev):
+        """build_Q_matrix with the start vectors in device memory: a
+        contiguous (p, dim) float64 CUDA tensor (or any object with .shape
+        and .data_ptr())."""
+        p = int(phi_dev.shape[0])
+        if self.dim == 0 or p == 0:
+            return np.zeros(0), np.zeros((p, 0))
+        if tuple(phi_dev.shape) != (p, self.dim):
+            raise ValueError("start vectors must have shape (p, dim)")
+        M = max(int(14 * p * math.log(1.0 * self.dim)), 2)
+        return self._band_lanczos(p, phi_dev.data_ptr(), M, lib().qcmg_band_lanczos_device)
+
+    def _band_lanczos(self, p, phi_ptr, M, fn):
         cap = GLOBAL["max_iter_BL"] + 2 * p + 2
         ev = np.zeros(cap)
         Q = np.zeros(p * cap)
         Mo = _lib.c_int()
-        check(lib().qcmg_band_lanczos(self._h, p, ptr(phis), M, GLOBAL["max_iter_BL"],
-                                      GLOBAL["accur_deflation"], GLOBAL["accur_band_lanczos"],
-                                      Mo, ptr(ev), ptr(Q), cap))
+        check(fn(self._h, p, phi_ptr, M, GLOBAL["max_iter_BL"], GLOBAL["accur_deflation"],
+                 GLOBAL["accur_band_lanczos"], Mo, ptr(ev), ptr(Q), cap))
         m = Mo.value
         return ev[:m].copy(), Q[: p * m].reshape(p, m).copy()
 
@@ -274,6 +288,36 @@ def apply_c(L, orb, pm, nup, ndn, x, z=1.0):
     y = np.zeros(n2)
     check(lib().qcmg_apply_c(L, orb, pm, nup, ndn, ptr(as_f64(x)), ptr(y), z, 0))
     return y
+
+
+def _cuda_ready():
+    """True when torch can hold device vectors for the library (the device
+    path of the Green-function set-up); the host path is the fallback when
+    torch has no GPU, e.g. for tests of the host logic."""
+    try:
+        import torch
+    except ImportError:
+        return False
+    return torch.cuda.is_available()
+
+
+def apply_c_device(L, orbs, pm, nup, ndn, x_dev):
+    """c_orb (pm=-1) / c^dagger_orb (pm=+1) of every orbital in orbs applied
+    to the device vector x_dev, on the device: a (len(orbs), dim') CUDA
+    tensor (dim' of the target sector)."""
+    import torch
+    spin = orbs[0] >= L
+    nup2, ndn2 = nup + (0 if spin else pm), ndn + (pm if spin else 0)
+    if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
+        return torch.zeros((len(orbs), 0), dtype=torch.float64, device=x_dev.device)
+    n2 = math.comb(L, nup2) * math.comb(L, ndn2)
+    out = torch.empty((len(orbs), n2), dtype=torch.float64, device=x_dev.device)
+    for k, orb in enumerate(orbs):
+        if (orb >= L) != spin:
+            raise ValueError("orbitals of one call must have the same spin")
+        check(lib().qcmg_apply_c(L, orb, pm, nup, ndn, x_dev.data_ptr(), out[k].data_ptr(), 1.0,
+                                 _lib.QCMG_DEVICE_PTRS))
+    return out
 
 
 def halfbasis(L, N):
@@ -407,8 +451,15 @@ class ModelInstance:
             H = self.hamiltonian(nup2, ndn2)
             if H.dim == 0:
                 continue
-            phi = [apply_c(L, o + spin * L, pm, st.sec.nup, st.sec.ndn, st.psi) for o in range(ns)]
-            e, Q = H.build_Q_matrix(phi)
+            if _cuda_ready():
+                # c / c^dagger applied on the device, start vectors left there
+                e, Q = H.build_Q_matrix_device(
+                    apply_c_device(L, [o + spin * L for o in range(ns)], pm, st.sec.nup,
+                                   st.sec.ndn, self._psi_device(st)))
+            else:
+                phi = [apply_c(L, o + spin * L, pm, st.sec.nup, st.sec.ndn, st.psi)
+                       for o in range(ns)]
+                e, Q = H.build_Q_matrix(phi)
             e = e - st.energy
             if pm == -1:
                 e = -e
@@ -422,6 +473,16 @@ class ModelInstance:
         v = np.concatenate(vs, axis=1) if vs else np.zeros((ns, 0), np.complex128)
         self._check_norm(v)
         return e, v * math.sqrt(st.weight)
+
+    @staticmethod
+    def _psi_device(st):
+        """The state's vector as a device tensor, uploaded once per state."""
+        import torch
+        d = getattr(st, "_psi_dev", None)
+        if d is None:
+            d = torch.from_numpy(np.ascontiguousarray(st.psi, np.float64)).to("cuda")
+            st._psi_dev = d
+        return d
 
     @staticmethod
     def _check_norm(v):

@@ -107,6 +107,27 @@ def test_create_destroy_bit_exact(pg):
         assert np.array_equal(y, g[tag + "_y"]), tag
 
 
+def test_device_start_vectors_match_host_path(pg):
+    """c / c^dagger applied on the device with the start vectors left there
+    (apply_c_device + build_Q_matrix_device) gives bit for bit the host
+    path's vectors and Q-matrix (apply_c + build_Q_matrix)."""
+    torch = _torch()
+    m, params, sec = engine_model("chain8")
+    inst = pg.ModelInstance(m, params, sec)
+    inst.ground_state()
+    st = inst.states[0]
+    L, ns = m.n_orb, m.n_sites
+    for pm in (-1, 1):
+        H = inst.hamiltonian(st.sec.nup + pm, st.sec.ndn)
+        phi = [pg.apply_c(L, o, pm, st.sec.nup, st.sec.ndn, st.psi) for o in range(ns)]
+        phi_d = pg.ed.apply_c_device(L, list(range(ns)), pm, st.sec.nup, st.sec.ndn,
+                                     torch.from_numpy(st.psi).cuda())
+        assert np.array_equal(phi_d.cpu().numpy(), np.array(phi))
+        e_h, Q_h = H.build_Q_matrix(phi)
+        e_d, Q_d = H.build_Q_matrix_device(phi_d)
+        assert np.array_equal(e_h, e_d) and np.array_equal(Q_h, Q_d), pm
+
+
 @pytest.mark.parametrize("tag", [t for t in CASES if CASES[t][6]])
 def test_green_function_pipeline(pg, tag):
     """ground state -> c/c^dagger -> band Lanczos -> Q-matrix -> G(z), all on
