@@ -150,6 +150,9 @@ struct PointArgs {
   const double* gpos;  // L x 3 (CPT)
   double2* out;        // MODE 1: nw x nk;  MODE 2: partial sums
   double* part;        // MODE 0: partial sums per block
+  int bpf;             // MODE 0: > 0: blocks per frequency (block b works on
+                       // frequency b / bpf only, so partials never mix
+                       // frequencies); 0: one flat range over all points
 };
 
 __device__ __forceinline__ void point_K(const PointArgs& A, int ik, double* K) {
@@ -175,7 +178,15 @@ __global__ void k_points(PointArgs A) {
 #define MI(r, c) mi[((r) * L + (c)) * T + t]
   const size_t npts = (size_t)A.nk * A.nw;
   double acc = 0.0;
-  for (size_t pt = blockIdx.x * (size_t)T + t; pt < npts + 0 * T; pt += (size_t)gridDim.x * T) {
+  // points of this block: a flat range, or (bpf > 0) the K points of one
+  // frequency, strided by the frequency's blocks
+  const bool per_freq = MODE == 0 && A.bpf > 0;
+  const size_t w_blk = per_freq ? blockIdx.x / A.bpf : 0;
+  const size_t first = per_freq ? w_blk * A.nk + (blockIdx.x % A.bpf) * (size_t)T + t
+                                : blockIdx.x * (size_t)T + t;
+  const size_t last = per_freq ? (w_blk + 1) * A.nk : npts;
+  const size_t step = per_freq ? (size_t)A.bpf * T : (size_t)gridDim.x * T;
+  for (size_t pt = first; pt < last; pt += step) {
     const int w = (int)(pt / A.nk), ik = (int)(pt % A.nk);
     double K[3];
     point_K(A, ik, K);
@@ -352,6 +363,7 @@ static PointArgs point_args(const Lattice& lat, int nw) {
   A.gpos = lat.gpos.p;
   A.out = nullptr;
   A.part = nullptr;
+  A.bpf = 0;
   return A;
 }
 
@@ -373,26 +385,34 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   const size_t smem = (size_t)2 * L * L * T * 8;
   QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DevBuf<double> part;
-  for (int i = 0; i < nw; ++i) {
-    PointArgs A = point_args(*this, 1);
-    A.base = (const double2*)base.p + (size_t)i * L * L;
+  // Several frequencies per launch (enough blocks for many waves on every
+  // SM), with each block's partial sum tied to one frequency, so the
+  // weights are still applied to whole per-frequency sums.
+  const unsigned bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
+  const int fpl = std::max(1, std::min(nw, (int)((152u * 16u + bpf - 1) / bpf)));
+  part.alloc((size_t)bpf * fpl);
+  std::vector<double> hp((size_t)bpf * fpl);
+  for (int i0 = 0; i0 < nw; i0 += fpl) {
+    const int nf = std::min(fpl, nw - i0);
+    PointArgs A = point_args(*this, nf);
+    A.base = (const double2*)base.p + (size_t)i0 * L * L;
     A.nk = nk;
     A.gx = nkx;
     A.gy = nky;
     A.gz = nkz;
     A.off = 0.0;
-    unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
-    part.alloc(g);
     A.part = part.p;
-    k_points<0><<<g, T, smem, s>>>(A);
+    A.bpf = (int)bpf;
+    k_points<0><<<bpf * nf, T, smem, s>>>(A);
     QCMG_CUDA(cudaGetLastError());
-    std::vector<double> hp(g);
-    QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, g * 8, cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
-    double sk = 0.0;
-    for (double v : hp) sk += v;
-    // log|det(VG - 1)| = log|det M| + log|det G|
-    total += wt[i] * (sk / nk + ldg[i]);
+    for (int f = 0; f < nf; ++f) {
+      double sk = 0.0;
+      for (unsigned b = 0; b < bpf; ++b) sk += hp[(size_t)f * bpf + b];
+      // log|det(VG - 1)| = log|det M| + log|det G|
+      total += wt[i0 + f] * (sk / nk + ldg[i0 + f]);
+    }
   }
   return total;
 }
