@@ -296,13 +296,15 @@ __global__ void k_points(PointArgs A) {
     }
   }
   if (MODE == 0) {
-    // block reduction of the log sums, fixed order
-    __shared__ double red[1024];
-    red[t] = acc;
+    // block reduction of the log sums, fixed order, in the (now free)
+    // matrix storage: the kernel has no static shared memory, so the whole
+    // opt-in budget can hold matrices
+    __syncthreads();
+    smem[t] = acc;
     __syncthreads();
     if (t == 0) {
       double s = 0.0;
-      for (int i = 0; i < T; ++i) s += red[i];
+      for (int i = 0; i < T; ++i) s += smem[i];
       A.part[blockIdx.x] = s;
     }
   }
@@ -314,8 +316,10 @@ __global__ void k_points(PointArgs A) {
 // host side
 
 static int point_threads(int L) {
+  // one L x L complex matrix per thread in shared memory, up to 224 KB a
+  // block (one block per SM at L = 12: 96 points)
   const size_t per = (size_t)2 * L * L * 8;  // bytes per point
-  int T = (int)((180 * 1024) / per);
+  int T = (int)((224 * 1024) / per);
   T = (T / 32) * 32;
   if (T > 256) T = 256;
   if (T < 32) T = 32;
