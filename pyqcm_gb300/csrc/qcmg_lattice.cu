@@ -18,6 +18,7 @@
 // with its matrix in shared memory (interleaved across threads, no bank
 // conflicts).
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "qcmg_internal.h"
@@ -320,6 +321,10 @@ static int point_threads(int L) {
   // block (one block per SM at L = 12: 96 points)
   const size_t per = (size_t)2 * L * L * 8;  // bytes per point
   int T = (int)((224 * 1024) / per);
+  if (const char* e = std::getenv("QCMG_POINT_THREADS")) {  // tuning override
+    const int v = std::atoi(e);
+    if (v >= 32 && (size_t)v * per <= 224 * 1024) T = v;
+  }
   T = (T / 32) * 32;
   if (T > 256) T = 256;
   if (T < 32) T = 32;
