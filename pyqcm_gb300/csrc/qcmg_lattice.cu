@@ -154,6 +154,7 @@ struct PointArgs {
   int bpf;             // MODE 0: > 0: blocks per frequency (block b works on
                        // frequency b / bpf only, so partials never mix
                        // frequencies); 0: one flat range over all points
+  const double* ldg;   // MODE 0: log|det G| per frequency, added point by point
 };
 
 __device__ __forceinline__ void point_K(const PointArgs& A, int ik, double* K) {
@@ -248,7 +249,11 @@ __global__ void k_points(PointArgs A) {
       }
     }
     if (MODE == 0) {
-      acc += logabs;  // weighted and combined with log|det G| by the reduction
+      // log|det(VG - 1)| = log|det M| + log|det G|, formed point by point:
+      // at high frequencies both terms are ~L log|z| and their sum is tiny,
+      // so summing the large terms over K first would leave the result to
+      // the rounding of that sum
+      acc += logabs + (A.ldg ? A.ldg[w] : 0.0);
       (void)perm;
     } else if (MODE == 1) {
       // y = M^-1 u, u_b = e^{2 pi i K.x_b};  g = (1/L) u^+ y
@@ -373,6 +378,7 @@ static PointArgs point_args(const Lattice& lat, int nw) {
   A.out = nullptr;
   A.part = nullptr;
   A.bpf = 0;
+  A.ldg = nullptr;
   return A;
 }
 
@@ -388,8 +394,6 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   // frequencies are processed one by one so the per-frequency weight is
   // applied exactly; each launch covers the whole K grid
   prepare(nw, z.data(), s);
-  std::vector<double> ldg(nw);
-  QCMG_CUDA(cudaMemcpyAsync(ldg.data(), logdetG.p, nw * 8, cudaMemcpyDeviceToHost, s));
   const int T = point_threads(L);
   const size_t smem = (size_t)2 * L * L * T * 8;
   QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -412,6 +416,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     A.off = 0.0;
     A.part = part.p;
     A.bpf = (int)bpf;
+    A.ldg = logdetG.p + i0;
     k_points<0><<<bpf * nf, T, smem, s>>>(A);
     QCMG_CUDA(cudaGetLastError());
     QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
@@ -419,8 +424,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     for (int f = 0; f < nf; ++f) {
       double sk = 0.0;
       for (unsigned b = 0; b < bpf; ++b) sk += hp[(size_t)f * bpf + b];
-      // log|det(VG - 1)| = log|det M| + log|det G|
-      total += wt[i0 + f] * (sk / nk + ldg[i0 + f]);
+      total += wt[i0 + f] * (sk / nk);
     }
   }
   return total;
