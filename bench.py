@@ -162,7 +162,9 @@ def run_reference(args):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
-    steps = max(1, args.steps)
+    # a bounded sample: each CPU product takes ~0.5 s on 16 Arm cores, so at
+    # most 20 of them are timed whatever --steps asks of the device arm
+    steps = max(1, min(args.steps, 20))
     gbs, dt = cpu_port_timing(steps, threads)
     sample = f"{steps} full products y += H x on the 4x4 N=16 Sz=0 sector, {threads} threads"
     line = {"impl": "reference", "metric": METRIC, "value": gbs, "unit": UNIT, "n_gpus": args.gpus,
@@ -519,7 +521,7 @@ def run_warmstart(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=200)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="qcmg", choices=["qcmg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
