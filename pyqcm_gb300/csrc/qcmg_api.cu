@@ -561,12 +561,30 @@ int qcmg_lattice_create(int L, int nR, const double* R, int nel, const int32_t* 
       t.R.upload(R, (size_t)3 * nR, t.stream);
       t.gpos.upload(gpos, (size_t)3 * L, t.stream);
       t.hdiff.upload(hdiff, (size_t)2 * L * L, t.stream);
-      std::vector<int> r(el_r, el_r + nel), c(el_c, el_c + nel), n(el_n, el_n + nel);
+      // elements grouped by translation: each point then computes one phase
+      // per translation instead of one per element
+      std::vector<int> order(nel);
+      for (int k = 0; k < nel; ++k) order[k] = k;
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return el_n[a] < el_n[b]; });
+      std::vector<int> r(nel), c(nel), n(nel), start(nR + 1, 0);
+      std::vector<double> v((size_t)2 * nel);
+      for (int k = 0; k < nel; ++k) {
+        const int o = order[k];
+        r[k] = el_r[o];
+        c[k] = el_c[o];
+        n[k] = el_n[o];
+        v[2 * k] = el_v[2 * o];
+        v[2 * k + 1] = el_v[2 * o + 1];
+        start[n[k] + 1]++;
+      }
+      for (int q = 0; q < nR; ++q) start[q + 1] += start[q];
+      t.el_start.upload(start.data(), nR + 1, t.stream);
+      t.R_host.assign(R, R + (size_t)3 * nR);
       if (nel) {
         t.el_r.upload(r.data(), nel, t.stream);
         t.el_c.upload(c.data(), nel, t.stream);
         t.el_n.upload(n.data(), nel, t.stream);
-        t.el_v.upload(el_v, (size_t)2 * nel, t.stream);
+        t.el_v.upload(v.data(), (size_t)2 * nel, t.stream);
       }
       QCMG_CUDA(cudaStreamSynchronize(t.stream));
     } catch (...) {

@@ -155,6 +155,8 @@ struct PointArgs {
                        // frequency b / bpf only, so partials never mix
                        // frequencies); 0: one flat range over all points
   const double* ldg;   // MODE 0: log|det G| per frequency, added point by point
+  const int* el_start;  // nR + 1 element ranges per translation
+  const double2* tab;   // grid phase tables (gx + gy + gz) x nR, or null: sincos per point
 };
 
 __device__ __forceinline__ void point_K(const PointArgs& A, int ik, double* K) {
@@ -198,16 +200,32 @@ __global__ void k_points(PointArgs A) {
       mr[e * T + t] = b.x;
       mi[e * T + t] = b.y;
     }
-    for (int e = 0; e < A.nel; ++e) {
-      const double* Rn = A.R + 3 * A.el_n[e];
-      double ph = 2.0 * M_PI * (K[0] * Rn[0] + K[1] * Rn[1] + K[2] * Rn[2]);
+    // M = Base - sum_e v_e e^{2 pi i K.R_n(e)} at (r_e, c_e), one phase per
+    // translation: on a grid the product of the three axes' table entries,
+    // else a sincos
+    for (int n = 0; n < A.nR; ++n) {
+      const int e0 = A.el_start[n], e1 = A.el_start[n + 1];
+      if (e0 == e1) continue;
       double s, c;
-      sincos(ph, &s, &c);
-      double2 v = A.el_v[e];
-      // M = Base - v e^{i ph} at (r, c)
-      int r = A.el_r[e], cc = A.el_c[e];
-      MR(r, cc) -= v.x * c - v.y * s;
-      MI(r, cc) -= v.x * s + v.y * c;
+      if (A.tab) {
+        const int ix = ik % A.gx, iy = (ik / A.gx) % A.gy, iz = ik / (A.gx * A.gy);
+        const double2 tx = A.tab[(size_t)ix * A.nR + n];
+        const double2 ty = A.tab[(size_t)(A.gx + iy) * A.nR + n];
+        const double2 tz = A.tab[(size_t)(A.gx + A.gy + iz) * A.nR + n];
+        const double xr = tx.x * ty.x - tx.y * ty.y, xi = tx.x * ty.y + tx.y * ty.x;
+        c = xr * tz.x - xi * tz.y;
+        s = xr * tz.y + xi * tz.x;
+      } else {
+        const double* Rn = A.R + 3 * n;
+        const double ph = 2.0 * M_PI * (K[0] * Rn[0] + K[1] * Rn[1] + K[2] * Rn[2]);
+        sincos(ph, &s, &c);
+      }
+      for (int e = e0; e < e1; ++e) {
+        const double2 v = A.el_v[e];
+        const int r = A.el_r[e], cc = A.el_c[e];
+        MR(r, cc) -= v.x * c - v.y * s;
+        MI(r, cc) -= v.x * s + v.y * c;
+      }
     }
     // LU with partial pivoting (row interchanges), in place.
     int perm[32];
@@ -379,7 +397,36 @@ static PointArgs point_args(const Lattice& lat, int nw) {
   A.part = nullptr;
   A.bpf = 0;
   A.ldg = nullptr;
+  A.el_start = lat.el_start.p;
+  A.tab = nullptr;
   return A;
+}
+
+const double* Lattice::phase_tables(int gx, int gy, int gz, double off, cudaStream_t s) {
+  if (tab.p && gx == tab_gx && gy == tab_gy && gz == tab_gz && off == tab_off) return tab.p;
+  // K = ((i + off)/gx, gy > 1 ? (j + off)/gy : 0, gz > 1 ? (l + off)/gz : 0), as point_K
+  std::vector<double> h((size_t)2 * (gx + gy + gz) * nR);
+  auto fill = [&](int base, int g, int axis) {
+    for (int i = 0; i < g; ++i) {
+      const double k = (axis == 0 || g > 1) ? (i + off) / g : 0.0;
+      for (int n = 0; n < nR; ++n) {
+        const double ph = 2.0 * M_PI * k * R_host[3 * n + axis];
+        const size_t at = ((size_t)(base + i) * nR + n) * 2;
+        h[at] = std::cos(ph);
+        h[at + 1] = std::sin(ph);
+      }
+    }
+  };
+  fill(0, gx, 0);
+  fill(gx, gy, 1);
+  fill(gx + gy, gz, 2);
+  tab.upload(h.data(), h.size(), s);
+  QCMG_CUDA(cudaStreamSynchronize(s));
+  tab_gx = gx;
+  tab_gy = gy;
+  tab_gz = gz;
+  tab_off = off;
+  return tab.p;
 }
 
 double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int nky, int nkz,
@@ -398,6 +445,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   const size_t smem = (size_t)2 * L * L * T * 8;
   QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DevBuf<double> part;
+  const double2* phases = (const double2*)phase_tables(nkx, nky, nkz, 0.0, s);
   // Several frequencies per launch (enough blocks for many waves on every
   // SM), with each block's partial sum tied to one frequency, so the
   // weights are still applied to whole per-frequency sums.
@@ -417,6 +465,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     A.part = part.p;
     A.bpf = (int)bpf;
     A.ldg = logdetG.p + i0;
+    A.tab = phases;
     k_points<0><<<bpf * nf, T, smem, s>>>(A);
     QCMG_CUDA(cudaGetLastError());
     QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
@@ -481,6 +530,7 @@ void Lattice::projected(int nw, const double* w, int kside, int dimk, double* pg
   nk = A.gx * A.gy * A.gz;
   A.nk = nk;
   A.off = dimk >= 1 ? 0.5 : 0.0;
+  A.tab = (const double2*)phase_tables(A.gx, A.gy, A.gz, A.off, s);
   const int LL = L * L;
   DevBuf<double> inv, out;
   inv.alloc((size_t)2 * nw * nk * LL);

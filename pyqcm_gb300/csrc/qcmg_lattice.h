@@ -15,8 +15,16 @@ struct Lattice {
   DevBuf<double> R;      // nR x 3, reduced superlattice coordinates
   DevBuf<double> gpos;   // L x 3, reduced coordinates
   DevBuf<double> hdiff;  // L x L complex, row-major
-  DevBuf<int> el_r, el_c, el_n;
+  DevBuf<int> el_r, el_c, el_n;  // grouped by translation n (stable order within a group)
   DevBuf<double> el_v;   // nel complex
+  DevBuf<int> el_start;  // nR + 1: the elements of translation n are [el_start[n], el_start[n+1])
+  std::vector<double> R_host;
+  // phase tables of a K grid, e^{2 pi i K_x R_n,x} per grid index and n (and
+  // likewise for y, z), cached for the last grid asked for
+  DevBuf<double> tab;
+  int tab_gx = 0, tab_gy = 0, tab_gz = 0;
+  double tab_off = -1.0;
+  const double* phase_tables(int gx, int gy, int gz, double off, cudaStream_t s);
   int M = -1;
   DevBuf<double> e;      // M poles
   DevBuf<double> v;      // L x M complex, column-major
