@@ -336,123 +336,6 @@ __global__ void k_points(PointArgs A) {
 #undef MI
 }
 
-// SEF integrand with four lanes per matrix.  One thread per matrix leaves
-// three warps per SM at L = 12 (the matrices fill shared memory) and the
-// kernel then waits on FP64 latency; here lane g of a matrix's group owns
-// the columns c = g (mod 4), so the same shared memory serves four times the
-// warps.  The eight matrices of a warp sit in lanes mi + 8 g; with a matrix
-// stride NM = 8 (mod 16) doubles, a warp's access to one (r, c) of its eight
-// matrices from the four column lanes touches 32 distinct 8-byte banks.
-// Per point the arithmetic is the single-lane kernel's, in the same order:
-// the owner of column p searches the pivot and forms the multipliers, every
-// lane updates its own columns.  part[block] = sum over the block's points
-// of log|det M| + log|det G| (one frequency per block, A.bpf blocks each).
-__global__ void __launch_bounds__(1024) k_sef_points(PointArgs A, int NM) {
-  extern __shared__ double smem[];
-  const int L = A.L, LL = L * L;
-  const int lane = threadIdx.x & 31;
-  const int g = lane >> 3;                          // column lane
-  const int mi = (threadIdx.x >> 5) * 8 + (lane & 7);  // matrix slot in the block
-  const int src0 = lane & 7;                        // lane of column lane 0 of this matrix
-  double* xr = smem;
-  double* xi = smem + (size_t)LL * NM;
-#define XR(r, c) xr[((r) * L + (c)) * NM + mi]
-#define XI(r, c) xi[((r) * L + (c)) * NM + mi]
-  const size_t w = blockIdx.x / A.bpf, kb = blockIdx.x % A.bpf;
-  const double2* B = A.base + w * LL;
-  const double ldg = A.ldg[w];
-  double acc = 0.0;
-  for (size_t k0 = kb * (size_t)NM; k0 < (size_t)A.nk; k0 += (size_t)A.bpf * NM) {
-    // every lane runs every step (the shuffles need the whole warp); slots
-    // past the grid's end factorize point 0 and are not counted
-    const bool live = k0 + mi < (size_t)A.nk;
-    const int ik = live ? (int)(k0 + mi) : 0;
-    for (int r = 0; r < L; ++r)
-      for (int c = g; c < L; c += 4) {
-        const double2 b = B[r * L + c];
-        XR(r, c) = b.x;
-        XI(r, c) = b.y;
-      }
-    const int ix = ik % A.gx, iy = (ik / A.gx) % A.gy, iz = ik / (A.gx * A.gy);
-    for (int n = 0; n < A.nR; ++n) {
-      const int e0 = A.el_start[n], e1 = A.el_start[n + 1];
-      if (e0 == e1) continue;
-      const double2 tx = A.tab[(size_t)ix * A.nR + n];
-      const double2 ty = A.tab[(size_t)(A.gx + iy) * A.nR + n];
-      const double2 tz = A.tab[(size_t)(A.gx + A.gy + iz) * A.nR + n];
-      const double pr = tx.x * ty.x - tx.y * ty.y, pi = tx.x * ty.y + tx.y * ty.x;
-      const double c = pr * tz.x - pi * tz.y, s = pr * tz.y + pi * tz.x;
-      for (int e = e0; e < e1; ++e) {
-        const int cc = A.el_c[e];
-        if ((cc & 3) != g) continue;
-        const double2 v = A.el_v[e];
-        const int r = A.el_r[e];
-        XR(r, cc) -= v.x * c - v.y * s;
-        XI(r, cc) -= v.x * s + v.y * c;
-      }
-    }
-    __syncwarp();
-    double logabs = 0.0;
-    for (int p = 0; p < L; ++p) {
-      const int owner = p & 3;
-      int best = p;
-      double bv = 0.0;
-      if (g == owner) {
-        bv = XR(p, p) * XR(p, p) + XI(p, p) * XI(p, p);
-        for (int r = p + 1; r < L; ++r) {
-          const double m = XR(r, p) * XR(r, p) + XI(r, p) * XI(r, p);
-          if (m > bv) {
-            bv = m;
-            best = r;
-          }
-        }
-      }
-      best = __shfl_sync(0xffffffffu, best, src0 + 8 * owner);
-      bv = __shfl_sync(0xffffffffu, bv, src0 + 8 * owner);
-      logabs += 0.5 * log(bv);
-      if (best != p)
-        for (int c = g; c < L; c += 4) {
-          const double a = XR(p, c), b = XI(p, c);
-          XR(p, c) = XR(best, c);
-          XI(p, c) = XI(best, c);
-          XR(best, c) = a;
-          XI(best, c) = b;
-        }
-      __syncwarp();
-      if (g == owner) {
-        const cdbl ip = cinv({XR(p, p), XI(p, p)});
-        for (int r = p + 1; r < L; ++r) {
-          const cdbl f = cmul({XR(r, p), XI(r, p)}, ip);
-          XR(r, p) = f.x;
-          XI(r, p) = f.y;
-        }
-      }
-      __syncwarp();
-      for (int c = (p + 1) + ((g - (p + 1)) & 3); c < L; c += 4) {  // own columns c > p
-        const double pr = XR(p, c), pi = XI(p, c);
-        for (int r = p + 1; r < L; ++r) {
-          const cdbl v = cfma_sub({XR(r, c), XI(r, c)}, {XR(r, p), XI(r, p)}, {pr, pi});
-          XR(r, c) = v.x;
-          XI(r, c) = v.y;
-        }
-      }
-      __syncwarp();
-    }
-    if (live && g == 0) acc += logabs + ldg;
-  }
-  // block sum in fixed order, in the freed matrix storage
-  __syncthreads();
-  smem[threadIdx.x] = acc;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double s = 0.0;
-    for (unsigned i = 0; i < blockDim.x; ++i) s += smem[i];
-    A.part[blockIdx.x] = s;
-  }
-#undef XR
-#undef XI
-}
-
 // ---------------------------------------------------------------------------
 // host side
 
@@ -558,21 +441,15 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   // frequencies are processed one by one so the per-frequency weight is
   // applied exactly; each launch covers the whole K grid
   prepare(nw, z.data(), s);
-  // k_sef_points: NM matrices per block (four lanes each), NM = 8 (mod 16)
-  // for conflict-free shared-memory access, within 224 KB and 1024 threads
-  const size_t per = (size_t)2 * L * L * 8;
-  int NM = 8;
-  for (int c = 8; c <= 248; c += 16)
-    if ((size_t)c * per <= 224 * 1024) NM = c;
-  const int T = 4 * NM;
-  const size_t smem = std::max((size_t)NM * per, (size_t)T * 8);
-  QCMG_CUDA(cudaFuncSetAttribute(k_sef_points, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  const int T = point_threads(L);
+  const size_t smem = (size_t)2 * L * L * T * 8;
+  QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
   DevBuf<double> part;
   const double2* phases = (const double2*)phase_tables(nkx, nky, nkz, 0.0, s);
   // Several frequencies per launch (enough blocks for many waves on every
   // SM), with each block's partial sum tied to one frequency, so the
   // weights are still applied to whole per-frequency sums.
-  const unsigned bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + NM - 1) / NM, 152 * 4));
+  const unsigned bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
   const int fpl = std::max(1, std::min(nw, (int)((152u * 16u + bpf - 1) / bpf)));
   part.alloc((size_t)bpf * fpl);
   std::vector<double> hp((size_t)bpf * fpl);
@@ -589,7 +466,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     A.bpf = (int)bpf;
     A.ldg = logdetG.p + i0;
     A.tab = phases;
-    k_sef_points<<<bpf * nf, T, smem, s>>>(A, NM);
+    k_points<0><<<bpf * nf, T, smem, s>>>(A);
     QCMG_CUDA(cudaGetLastError());
     QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
