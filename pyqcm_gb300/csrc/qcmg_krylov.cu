@@ -66,6 +66,41 @@ __global__ void __launch_bounds__(256) k_multidot(VL V, int m, const double* __r
   for (int k = threadIdx.x; k < m; k += blockDim.x) part[(size_t)blockIdx.x * m + k] = acc[k];
 }
 
+// The same partials for short lists, accumulated in registers: each thread
+// keeps m sums over its elements, so an element costs one load of w and m
+// independent loads and FMAs (no dependent chain per vector, no staging
+// barrier), and the block then reduces each sum in a fixed order.
+template <int MAXM>
+__global__ void __launch_bounds__(256) k_multidot_reg(VecList V, int m,
+                                                      const double* __restrict__ w, size_t n,
+                                                      double* __restrict__ part) {
+  double acc[MAXM];
+#pragma unroll
+  for (int k = 0; k < MAXM; ++k) acc[k] = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    const double wi = w[i];
+#pragma unroll
+    for (int k = 0; k < MAXM; ++k)
+      if (k < m) acc[k] = fma(V[k][i], wi, acc[k]);
+  }
+  __shared__ double red[8][MAXM];  // one row per warp of the 256-thread block
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+  for (int k = 0; k < MAXM; ++k) {
+    double v = acc[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) red[wp][k] = v;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    double t = 0.0;
+    for (int q = 0; q < 8; ++q) t += red[q][k];
+    part[(size_t)blockIdx.x * m + k] = t;
+  }
+}
+
 // out[k] = sum_b part[b*m + k], fixed order.
 __global__ void k_multidot_final(const double* __restrict__ part, int nb, int m,
                                  double* __restrict__ out) {
@@ -193,13 +228,27 @@ struct MultiOps {
     out.assign(m, 0.0);
     if (m == 0) return;
     nblocks = multidot_blocks(n);
-    part.alloc((size_t)nblocks * m);
-    coef.alloc(m);
-    if (m <= kByValue) {
+    if (m <= 32) {
+      // register accumulators: 256-thread blocks, two per SM at most
+      nblocks = (int)std::max<size_t>(1, std::min<size_t>((n + 255) / 256, 2 * 152));
+      part.alloc((size_t)nblocks * m);
+      VecList L;
+      for (int k = 0; k < m; ++k) L.v[k] = V[k];
+      if (m <= 4)
+        k_multidot_reg<4><<<nblocks, 256, 0, s>>>(L, m, w, n, part.p);
+      else if (m <= 8)
+        k_multidot_reg<8><<<nblocks, 256, 0, s>>>(L, m, w, n, part.p);
+      else if (m <= 16)
+        k_multidot_reg<16><<<nblocks, 256, 0, s>>>(L, m, w, n, part.p);
+      else
+        k_multidot_reg<32><<<nblocks, 256, 0, s>>>(L, m, w, n, part.p);
+    } else if (m <= kByValue) {
+      part.alloc((size_t)nblocks * m);
       VecList L;
       for (int k = 0; k < m; ++k) L.v[k] = V[k];
       k_multidot<VecList><<<nblocks, 256, m * sizeof(double), s>>>(L, m, w, n, part.p);
     } else {
+      part.alloc((size_t)nblocks * m);
       ptrs.alloc(m);
       QCMG_CUDA(cudaMemcpyAsync(ptrs.p, V.data(), m * sizeof(double*), cudaMemcpyHostToDevice, s));
       k_multidot<const double* const*>
