@@ -317,107 +317,6 @@ __device__ __forceinline__ void passD_accum(const int64_t* __restrict__ x, uint3
   }
 }
 
-// Pass D with the neighbour segments staged by bulk copies.  Work item =
-// (band of kD5Rows rows, down state a).  Warp 0 is the producer: it reads
-// a's neighbour list and bulk-copies each neighbour's band segment of x
-// (kD5Rows contiguous elements) into a stage of the shared ring; the other
-// warps sum the staged segments row by row (sequential, conflict-free
-// shared loads) and add the result into y.  The copies run ahead by up to
-// kD5Stages items, so L2 latency is hidden by the copy engine rather than
-// by loads in flight per thread.  Items run band-major over the grid, so
-// the band of x that all CTAs read at a time stays in L2.
-// Launch contract (launch_product checks it): du even (16-byte aligned
-// segments), every down state has at most kD5MaxNb neighbours, blockDim =
-// 32 + kD5Rows, dynamic shared memory kD5Smem bytes.
-constexpr int kD5Rows = 256;
-constexpr int kD5MaxNb = 32;
-constexpr int kD5Stages = 3;
-constexpr size_t kD5StageElems = (size_t)kD5MaxNb * kD5Rows;
-constexpr size_t kD5Smem = kD5Stages * kD5StageElems * sizeof(int64_t);
-
-template <bool FAST>
-__global__ void __launch_bounds__(32 + kD5Rows, 1) k_fx_passD5(FxProdArgs A) {
-  extern __shared__ __align__(128) int64_t ring[];
-  __shared__ __align__(8) uint64_t full[kD5Stages], empty[kD5Stages];
-  __shared__ int meta[kD5Stages][2];  // np, nt of the staged item
-  __shared__ int abort_flag;
-  const uint32_t du = A.du, dd = A.dd;
-  const int tid = threadIdx.x, lane = tid & 31;
-  const bool producer = tid < 32;
-  const uint32_t nbands = (du + kD5Rows - 1) / kD5Rows;
-  const size_t items = (size_t)nbands * dd;
-  if (tid == 0) {
-    for (int st = 0; st < kD5Stages; ++st) {
-      mbar_init(&full[st], 1);
-      mbar_init(&empty[st], kD5Rows);
-    }
-    abort_flag = 0;
-    fence_barrier_init();
-  }
-  __syncthreads();
-  size_t iter = 0;
-  for (size_t it = blockIdx.x; it < items; it += gridDim.x, ++iter) {
-    const int st = (int)(iter % kD5Stages);
-    const unsigned ph = (unsigned)((iter / kD5Stages) & 1u);
-    const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
-    const uint32_t r0 = band * kD5Rows, rows = min((uint32_t)kD5Rows, du - r0);
-    int64_t* buf = ring + (size_t)st * kD5StageElems;
-    if (producer) {
-      // the stage is free once its previous item's consumers have arrived
-      const bool ok = iter < (size_t)kD5Stages || mbar_wait_bounded(&empty[st], ph ^ 1u);
-      // warp-uniform decision: the lanes stay converged for the shuffles
-      if (__any_sync(0xffffffffu, !ok || *(volatile int*)&abort_flag)) {
-        if (lane == 0) {
-          abort_flag = 1;
-          atomicExch(A.err, 1);
-        }
-        break;
-      }
-      const uint32_t k0 = A.rp_dn[a];
-      const int np = (int)(A.rs_dn[a] - k0), nt = (int)(A.rp_dn[a + 1] - k0);
-      const uint32_t col = lane < nt ? A.col_dn[k0 + lane] : 0u;
-      const unsigned bytes = rows * 8u;
-      if (lane == 0) {
-        meta[st][0] = np;
-        meta[st][1] = nt;
-        fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&full[st], (unsigned)nt * bytes);
-      }
-      for (int k = 0; k < nt; ++k) {
-        const uint32_t b = __shfl_sync(0xffffffffu, col, k);
-        if (lane == 0) bulk_g2s(buf + (size_t)k * kD5Rows, A.x + (size_t)b * du + r0, bytes, &full[st]);
-      }
-    } else {
-      const int row = tid - 32;
-      bool ok = mbar_wait_bounded(&full[st], ph);
-      if (!ok || *(volatile int*)&abort_flag) {
-        if (row == 0) {
-          abort_flag = 1;
-          atomicExch(A.err, 1);
-        }
-        break;
-      }
-      const int np = meta[st][0], nt = meta[st][1];
-      if ((uint32_t)row < rows) {
-        int64_t P = 0, N = 0;
-        for (int k = 0; k < np; ++k) P += buf[(size_t)k * kD5Rows + row];
-        for (int k = np; k < nt; ++k) N += buf[(size_t)k * kD5Rows + row];
-        int64_t* yp = A.y + (size_t)a * du + r0 + row;
-        const int64_t t = FAST ? rshift_fixed(P - N, A.t_dn, A.r_dn) : mul_fix(P - N, A.mt_dn, A.sh_dn);
-        __stcs(yp, __ldcs(yp) + t);
-      }
-      mbar_arrive(&empty[st]);
-    }
-  }
-  // the producer leaves only after the copies it issued have landed (the
-  // CTA's shared memory must outlive them); bounded like every wait here
-  if (producer && lane == 0) {
-    const size_t issued = iter;
-    for (size_t j = issued > (size_t)kD5Stages ? issued - kD5Stages : 0; j < issued; ++j)
-      (void)mbar_wait_bounded(&full[j % kD5Stages], (unsigned)((j / kD5Stages) & 1u));
-  }
-}
-
 // VEC = 2 needs du even (every slab segment at an even row is 16-byte
 // aligned); bands start at multiples of 256 rows.  DOT: also the dot
 // product of the finished y with A.dot_x (the element of x at the same
@@ -690,19 +589,6 @@ unsigned launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStre
   // pass D
   const size_t items = (size_t)A.nbands * H->dd;
   const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * 8));
-  // staged pass D (QCMG_FX_PASSD=5): du even, down degree <= kD5MaxNb, no fused dot
-  static const char* passd_env = std::getenv("QCMG_FX_PASSD");
-  if (passd_env && std::atoi(passd_env) == 5 && (H->du & 1u) == 0u && T.maxdeg_dn <= kD5MaxNb &&
-      !A.dot_part) {
-    auto go = [&](auto kern) {
-      QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kD5Smem));
-      kern<<<sms, 32 + kD5Rows, kD5Smem, s>>>(A);
-    };
-    if (fast) go(k_fx_passD5<true>);
-    else go(k_fx_passD5<false>);
-    QCMG_CUDA(cudaGetLastError());
-    return (unsigned)sms;
-  }
   auto passD = [&](auto vec_tag, auto fast_tag) {
     constexpr int V = decltype(vec_tag)::value;
     constexpr bool F = decltype(fast_tag)::value;
