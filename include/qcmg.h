@@ -193,6 +193,16 @@ int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_targe
                       double acc_deflation, double acc_band, int* M, double* evals, double* Q,
                       int cap);
 
+/* Continued-fraction Lanczos from one normalized start vector psi (length
+ * dim; a device pointer with QCMG_DEVICE_PTRS): the three-term recurrence
+ * with the reference's stopping rule (the product of the b's or the last b
+ * at or below accur, or max_iter steps).  Outputs *n steps, a[n] and
+ * b[n + 1] with b[0] = 1; capacity cap >= n.  Replaces LanczosGreen
+ * (src_ed/Hamiltonian/Lanczos.hpp:156-183), called by
+ * model_instance<double>::build_cf (src_ed/model_instance.cpp:35-100). */
+int qcmg_lanczos_green(qcmg_hamiltonian* H, const double* psi, unsigned flags, double accur,
+                       int max_iter, int* n, double* a, double* b, int cap);
+
 /* qcmg_band_lanczos with the start vectors already in the handle's device
  * memory (p x dim, row-major; e.g. written there by qcmg_apply_c with
  * QCMG_DEVICE_PTRS), so they cross no host link.  The call waits for the

@@ -403,3 +403,93 @@ def qmatrix_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, orbitals, spin_down
     e = np.concatenate(blocks_e)
     v = np.concatenate(blocks_v, axis=1)
     return e, v
+
+
+# ----------------------------------------------------------------------------
+# Continued-fraction Green function (GF_method 'F')
+
+
+def lanczos_green(mult_add, psi, accur=0.01, max_iter=400):
+    """(a, b) of the reference's LanczosGreen (Lanczos.hpp:156-183): the
+    three-term recurrence from the normalized psi, stopped when the product
+    of the b's or the last b falls to accur, or after max_iter steps; b
+    starts with 1 and has one entry more than a."""
+    psi = np.array(psi, np.float64)
+    q = np.zeros(len(psi))
+    a, b = [], [1.0]
+    prod = 1.0
+    while prod > accur and abs(b[-1]) > accur and len(a) < max_iter:
+        if a:  # psi <- q / beta, q <- -beta psi (vector_num.hpp:274-282)
+            beta = b[-1]
+            psi, q = q * (1.0 / beta), -beta * psi
+        mult_add(psi, q)
+        z = float(psi @ q)
+        a.append(z)
+        q -= z * psi
+        zz = float(np.linalg.norm(q))
+        b.append(zz)
+        prod *= abs(zz)
+    return np.array(a), np.array(b)
+
+
+def continued_fraction(a, b, e0, norm, create):
+    """The reference's continued_fraction(a, b, e0, norm, create)
+    (continued_fraction.cpp:30-37): b -> b^2 with b[0] = norm, a shifted by
+    the ground-state energy (electron part a - e0, hole part e0 - a)."""
+    a = np.array(a, np.float64)
+    b = np.array(b, np.float64) ** 2
+    b[0] = norm
+    a = a - e0 if create else e0 - a
+    return a, b
+
+
+def cf_evaluate(a, b, z):
+    """G(z) = b0 / (z - a0 - b1 / (z - a1 - ...)) (continued_fraction.cpp:48-53)."""
+    G = 0.0 + 0.0j
+    for i in range(len(a) - 1, -1, -1):
+        G = b[i] / (z - a[i] - G)
+    return G
+
+
+def cf_green_function_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, weight, orbitals, zs,
+                                spin_down=False, accur=0.01, max_iter=400):
+    """G(z) of one ground state by continued fractions, real case, as
+    model_instance<double>::build_cf (model_instance.cpp:35-100) and
+    continued_fraction_set::Green_function (continued_fraction_set.cpp:63-98)
+    assemble it: a fraction per orbital pair (o2 <= o1) from c_o1 psi
+    (+ c_o2 psi), electron and hole parts; off-diagonal elements
+    0.5 (G_{o1+o2} - G_o1o1 - G_o2o2).  Returns (nz, L, L)."""
+    n = len(orbitals)
+    spin = 1 if spin_down else 0
+    frac = {}
+    for pm in (-1, 1):
+        nup2 = nup + (0 if spin else pm)
+        ndn2 = ndn + (pm if spin else 0)
+        if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L_orb:
+            continue
+        mult_add, dim = mult_add_of(nup2, ndn2)
+        if dim == 0:
+            continue
+        for i1, o1 in enumerate(orbitals):
+            for i2 in range(i1 + 1):
+                o2 = orbitals[i2]
+                x = apply_c(L_orb, o1 + spin * L_orb, pm, nup, ndn, psi)
+                if i2 != i1:
+                    x = x + apply_c(L_orb, o2 + spin * L_orb, pm, nup, ndn, psi)
+                norm = float(x @ x)
+                if norm > 1e-14:
+                    a, b = lanczos_green(mult_add, x / np.sqrt(norm), accur, max_iter)
+                    frac[(pm, i1, i2)] = continued_fraction(a, b, E0, norm * weight, pm == 1)
+    zs = np.atleast_1d(np.asarray(zs, np.complex128))
+    G = np.zeros((len(zs), n, n), np.complex128)
+    for w, z in enumerate(zs):
+        def part(i1, i2):
+            return sum(cf_evaluate(*frac[(pm, i1, i2)], z) for pm in (-1, 1) if (pm, i1, i2) in frac)
+        d = [part(i, i) for i in range(n)]
+        for i in range(n):
+            G[w, i, i] = d[i]
+        for i1 in range(n):
+            for i2 in range(i1):
+                t = 0.5 * (part(i1, i2) - d[i1] - d[i2])
+                G[w, i1, i2] = G[w, i2, i1] = t
+    return G

@@ -447,6 +447,24 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
   });
 }
 
+int qcmg_lanczos_green(qcmg_hamiltonian* H, const double* psi, unsigned flags, double accur,
+                       int max_iter, int* n, double* a, double* b, int cap) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && psi != nullptr && n != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(accur > 0.0 && max_iter > 0, "accur and max_iter must be positive");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    *n = 0;
+    const bool dev = (flags & QCMG_DEVICE_PTRS) != 0;
+    if (dev) QCMG_CUDA(cudaDeviceSynchronize());  // the vector may come from any stream
+    GreenResult r = lanczos_green(H, psi, dev, accur, max_iter);
+    *n = (int)r.a.size();
+    QCMG_CHECK_ARG(*n <= cap, "continued-fraction output capacity too small");
+    if (a) std::copy(r.a.begin(), r.a.end(), a);
+    if (b) std::copy(r.b.begin(), r.b.end(), b);
+  });
+}
+
 static int band_lanczos_entry(qcmg_hamiltonian* H, int p, const double* phi, bool on_device,
                               int M_target, int max_iter, double acc_deflation, double acc_band,
                               int* M, double* evals, double* Q, int cap) {

@@ -547,6 +547,43 @@ struct Cusolver {
   }
 };
 
+// LanczosGreen (src_ed/Hamiltonian/Lanczos.hpp:156-183): the three-term
+// recurrence from a normalized start vector, on device vectors with the
+// host keeping a and b; the reference's stopping rule (product of the b's
+// or the last b at or below accur, or max_iter steps).
+GreenResult lanczos_green(qcmg_hamiltonian* H, const double* psi0, bool on_device, double accur,
+                          int max_iter) {
+  const size_t n = H->dim;
+  cudaStream_t s = H->stream;
+  GreenResult out;
+  out.b.push_back(1.0);
+  if (n == 0) return out;
+  DevVec P(n), Q(n);
+  QCMG_CUDA(cudaMemcpyAsync(P.p, psi0, n * 8,
+                            on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  QCMG_CUDA(cudaMemsetAsync(Q.p, 0, n * 8, s));
+  double* pp = P.p;  // psi
+  double* qp = Q.p;  // q
+  Reducer red;
+  double prod = 1.0;
+  while (prod > accur && std::fabs(out.b.back()) > accur && (int)out.a.size() < max_iter) {
+    if (!out.a.empty()) {  // psi <- q / beta, q <- -beta psi
+      const double beta = out.b.back();
+      std::swap(pp, qp);
+      scale2(pp, 1.0 / beta, qp, -beta, n, s);
+    }
+    matvec(H, pp, qp, true);  // q += H psi
+    const double z = red.dot(pp, qp, n, s);
+    out.a.push_back(z);
+    const double zz = std::sqrt(red.axpy_norm2(qp, pp, z, n, s));  // q -= z psi
+    if (!std::isfinite(z) || !std::isfinite(zz))
+      throw Error(QCMG_ERR_NUMERIC, "continued-fraction Lanczos produced a non-finite value");
+    out.b.push_back(zz);
+    prod *= std::fabs(zz);
+  }
+  return out;
+}
+
 BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device, int M0,
                         int max_iter,
                         double acc_defl, double acc_band) {

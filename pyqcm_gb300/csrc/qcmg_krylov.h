@@ -28,6 +28,16 @@ void seeded_vector(size_t dim, unsigned seed, double* out);
 LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,
                                    double tol, int max_iter, int reorth, double* psi_host);
 
+struct GreenResult {
+  std::vector<double> a;  // n
+  std::vector<double> b;  // n + 1, b[0] = 1
+};
+
+// The continued-fraction Lanczos of one normalized start vector (host or
+// device memory).
+GreenResult lanczos_green(qcmg_hamiltonian* H, const double* psi0, bool on_device, double accur,
+                          int max_iter);
+
 // phi_in: p start vectors of length dim, vector k at phi_in + k*dim, in
 // host memory or (phi_on_device) in the handle's device memory.
 BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device,

@@ -34,6 +34,11 @@ GLOBAL = {
     "temperature": 0.0,
     "seed": 0,
     "Lanczos_reorth": 0,
+    # Green-function representation: 'L' Lehmann form from band Lanczos, 'F'
+    # continued fractions (src_util/global_parameter.cpp:61,76,90)
+    "GF_method": "L",
+    "accur_continued_fraction": 0.01,
+    "max_iter_CF": 400,
 }
 MIN_GAP = 1.0e-6      # src_ed/model.hpp:19
 SMALL_VALUE = 1e-12   # degeneracy threshold of compute_weights
@@ -244,6 +249,22 @@ class Hamiltonian:
             out.append(State(self.sec, e0, psi))
         return out, GS_energy
 
+    def lanczos_green(self, psi):
+        """(a, b) of the continued-fraction Lanczos from the normalized
+        psi: a host array, or a device tensor (anything with data_ptr())
+        (LanczosGreen, Lanczos.hpp:156-183)."""
+        cap = GLOBAL["max_iter_CF"] + 1
+        a, b = np.zeros(cap), np.zeros(cap + 1)
+        n = _lib.c_int()
+        if hasattr(psi, "data_ptr"):
+            p, flags = psi.data_ptr(), _lib.QCMG_DEVICE_PTRS
+        else:
+            p, flags = ptr(as_f64(psi)), 0
+        check(lib().qcmg_lanczos_green(self._h, p, flags, GLOBAL["accur_continued_fraction"],
+                                       GLOBAL["max_iter_CF"], n, ptr(a), ptr(b), cap))
+        m = n.value
+        return a[:m].copy(), b[: m + 1].copy()
+
     def build_Q_matrix(self, phi):
         """(e, Q) with Q of shape (p, M) (Hamiltonian_base.hpp:229-254)."""
         p = len(phi)
@@ -394,6 +415,9 @@ class ModelInstance:
         self.GS_energy = None
         self.E0 = None
         self._H = {}
+        self.gf_method = GLOBAL["GF_method"]
+        if self.gf_method not in ("L", "F"):
+            raise ValueError("GF_method must be 'L' (band Lanczos) or 'F' (continued fractions)")
 
     def hamiltonian(self, nup, ndn):
         key = (nup, ndn)
@@ -495,14 +519,86 @@ class ModelInstance:
         if self.gf_solved:
             return
         self.ground_state()
+        solve = self._cf_state if self.gf_method == "F" else self._qmatrix_state
         for st in self.states:
-            st.gf = self._qmatrix_state(st, False)
+            st.gf = solve(st, False)
             if self.mixing & 4:
-                st.gf_down = self._qmatrix_state(st, True)
+                st.gf_down = solve(st, True)
         self.gf_solved = True
+
+    def _cf_state(self, st, spin_down):
+        """Continued fractions of one state, as model_instance<double>::build_cf
+        (model_instance.cpp:35-100): for every orbital pair o2 <= o1, the
+        continued-fraction Lanczos from c_o1 psi (+ c_o2 psi), normalized,
+        for the electron (pm = +1) and hole (pm = -1) parts.  Returns
+        {(pm, o1, o2): (a, b)} in evaluation form (continued_fraction.cpp:30-37:
+        b squared with b[0] = |c psi|^2 * weight, a shifted by the energy)."""
+        L, ns = self.model.n_orb, self.model.n_sites
+        spin = 1 if spin_down else 0
+        frac = {}
+        for pm in (-1, 1):
+            nup2 = st.sec.nup + (0 if spin else pm)
+            ndn2 = st.sec.ndn + (pm if spin else 0)
+            if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
+                continue
+            H = self.hamiltonian(nup2, ndn2)
+            if H.dim == 0:
+                continue
+            orbs = [o + spin * L for o in range(ns)]
+            if _cuda_ready():
+                phi = apply_c_device(L, orbs, pm, st.sec.nup, st.sec.ndn, self._psi_device(st))
+            else:
+                phi = np.array([apply_c(L, o, pm, st.sec.nup, st.sec.ndn, st.psi) for o in orbs])
+            for o1 in range(ns):
+                for o2 in range(o1 + 1):
+                    x = phi[o1] + phi[o2] if o2 != o1 else phi[o1]
+                    norm = float((x * x).sum())
+                    if norm <= 1e-14:
+                        continue
+                    a, b = H.lanczos_green(x / math.sqrt(norm))
+                    b = b ** 2
+                    b[0] = norm * st.weight
+                    a = a - st.energy if pm == 1 else st.energy - a
+                    frac[(pm, o1, o2)] = (a, b)
+        return frac
+
+    def _cf_green(self, frac, zs):
+        """G(z) (nz, L, L) of one state's continued fractions
+        (continued_fraction_set::Green_function, real case,
+        continued_fraction_set.cpp:63-98): diagonal elements from the
+        (o, o) fractions, off-diagonal ones 0.5 (G_{o1+o2} - G_o1o1 - G_o2o2)."""
+        ns = self.model.n_sites
+        keys = list(frac)
+        nmax = max((len(frac[k][0]) for k in keys), default=0)
+        # all fractions at once, padded with b = 0 (a zero term leaves G as it is)
+        A = np.zeros((len(keys), nmax))
+        B = np.zeros((len(keys), nmax))
+        for i, k in enumerate(keys):
+            a, b = frac[k]
+            A[i, :len(a)] = a
+            B[i, :len(a)] = b[:len(a)]
+        val = np.zeros((len(keys), len(zs)), np.complex128)
+        for j in range(nmax - 1, -1, -1):
+            val = B[:, j, None] / (zs[None, :] - A[:, j, None] - val)
+        part = {}
+        for i, (pm, o1, o2) in enumerate(keys):
+            part[(o1, o2)] = part.get((o1, o2), 0.0) + val[i]
+        G = np.zeros((len(zs), ns, ns), np.complex128)
+        zero = np.zeros(len(zs), np.complex128)
+        d = [part.get((o, o), zero) for o in range(ns)]
+        for o in range(ns):
+            G[:, o, o] = d[o]
+        for o1 in range(ns):
+            for o2 in range(o1):
+                t = 0.5 * (part.get((o1, o2), zero) - d[o1] - d[o2])
+                G[:, o1, o2] = t
+                G[:, o2, o1] = t
+        return G
 
     def qmatrix(self, spin_down=False):
         """(e, v) of the first state, v of shape (L, M)."""
+        if self.gf_method != "L":
+            raise ValueError("the Q-matrix exists with GF_method 'L' only")
         self.Green_function_solve()
         st = self.states[0]
         return st.gf_down if (spin_down and self.mixing & 4) else st.gf
@@ -513,8 +609,8 @@ class ModelInstance:
         zs = np.atleast_1d(np.asarray(z, np.complex128))
         G = None
         for st in self.states:
-            e, v = st.gf_down if (spin_down and self.mixing & 4) else st.gf
-            g = green_function(e, v, zs)
+            gf = st.gf_down if (spin_down and self.mixing & 4) else st.gf
+            g = self._cf_green(gf, zs) if self.gf_method == "F" else green_function(*gf, zs)
             G = g if G is None else G + g
         return G[0] if np.ndim(z) == 0 else G
 

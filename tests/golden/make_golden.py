@@ -3,6 +3,7 @@ exact-diagonalization code (compiled by oracle/refbuild into oracle/_ref).
 
 Run from the repository root, in a container that has the reference tree:
     make -C oracle/refbuild && python tests/golden/make_golden.py
+(`python tests/golden/make_golden.py cf` makes the continued-fraction cases only.)
 Each case writes <case>.npz holding the spec it ran and every array the
 reference produced (see oracle/refbuild/ref_driver.cpp for the commands).
 """
@@ -78,9 +79,38 @@ def ed_case(tag, nx, ny, params, sector, n_bath=0, af=False, extra=(), gf=True, 
     print(tag, sorted(k for k in out if k != "spec"))
 
 
+# Cases run again with the continued-fraction Green function (GF_method 'F'):
+# G(z) on ZS from the reference's build_cf + continued_fraction_set.  The
+# reference's build_cf reads H->B->dim, which its factorized format leaves
+# null (src_ed/model_instance.cpp:51, a null dereference), so these run on
+# its sparse format 'S': the same Hamiltonian, stored as a CSR matrix.
+CF_CASES = ["chain8", "ladder2x4_af", "plaquette_bath4"]
+
+
+def cf_case(tag):
+    nx, ny, nb, af, params, sec, _ = CASES[tag]
+    ns, nb, ops = hubbard_cluster(nx, ny, nb, af)
+    lines = ["gchar Hamiltonian_format S", "gchar GF_method F", "gint seed 0"]
+    lines += model_lines("clus", ns, nb, ops)
+    lines += [f"param {k} {v!r}" for k, v in params.items() if k in ops]
+    lines += [f"instance clus {sec} 1"]
+    for k, z in enumerate(ZS):
+        lines += [f"gz 1 0 {z.real!r} {z.imag!r} gz{k}"]
+        if af:
+            lines += [f"gz 1 1 {z.real!r} {z.imag!r} gzdn{k}"]
+    lines += ["gs 1 gs"]
+    out = run_spec(lines)
+    np.savez_compressed(os.path.join(HERE, tag + "_cf.npz"), **out)
+    print(tag + "_cf", sorted(k for k in out if k != "spec"))
+
+
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference oracle first: make -C oracle/refbuild")
+    if sys.argv[1:] == ["cf"]:  # the continued-fraction cases only
+        for tag in CF_CASES:
+            cf_case(tag)
+        return
     # Half bases for L = 8, 12, 16 at half filling and one off-half filling.
     lines = ["halfbasis 8 4", "halfbasis 8 3", "halfbasis 12 6", "halfbasis 12 5", "halfbasis 16 8"]
     out = run_spec(lines)
@@ -93,6 +123,8 @@ def main():
         ed_case(tag, nx, ny, params, sec, n_bath=nb, af=af, extra=extra, gf=gf, gz=ZS)
     for tag, c in LATTICE_CASES.items():
         lattice_case(tag, c)
+    for tag in CF_CASES:
+        cf_case(tag)
 
 def lattice_case(tag, c):
     """Runs a lattice model through the reference's QCM layer."""

@@ -153,6 +153,30 @@ def test_green_function_pipeline(pg, tag):
             assert np.max(np.abs(inst.self_energy(z) - g[f"sig{k}"])) < 1e-7
 
 
+@pytest.mark.parametrize("tag", ["chain8", "ladder2x4_af", "plaquette_bath4"])
+def test_continued_fraction_green_function(pg, tag):
+    """GF_method 'F': ground state -> c/c^dagger per orbital pair ->
+    continued-fraction Lanczos on the GPU -> G(z), against the reference's
+    own continued-fraction G(z) (build_cf, continued_fraction_set)."""
+    g = load_golden(tag + "_cf")
+    m, params, sec = engine_model(tag)
+    pg.set_global_parameter("GF_method", "F")
+    try:
+        inst = pg.ModelInstance(m, params, sec)
+    finally:
+        pg.set_global_parameter("GF_method", "L")
+    E0, _ = inst.ground_state()
+    assert abs(E0 - g["gs_E0"]) <= 1e-10 * abs(g["gs_E0"])
+    af = CASES[tag][3]
+    for spin_down in ((False, True) if af else (False,)):
+        G = inst.Green_function(np.array(ZS), spin_down)
+        for k in range(len(ZS)):
+            ref = g[("gzdn" if spin_down else "gz") + str(k)]
+            assert np.max(np.abs(G[k] - ref)) < 1e-9, (tag, spin_down, k)
+    with pytest.raises(ValueError):
+        inst.qmatrix()
+
+
 def test_green_function_kernel_vs_numpy(pg):
     rng = np.random.default_rng(5)
     L, M = 12, 700

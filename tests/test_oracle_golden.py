@@ -119,3 +119,31 @@ def assert_qmatrix_parity(e, v, e_ref, v_ref, elow=2.0, wmin=1e-4, tol=1e-8):
         G = qo.green_function(e, v, z)
         Gr = qo.green_function(e_ref, v_ref, z)
         assert np.max(np.abs(G - Gr)) < tol, z
+
+
+@pytest.mark.parametrize("tag", ["chain8", "ladder2x4_af", "plaquette_bath4"])
+def test_continued_fraction_green_function_against_reference(tag):
+    """The oracle's restatement of the continued-fraction Green function
+    (GF_method 'F': LanczosGreen per orbital pair, Lanczos.hpp:156-183, and
+    continued_fraction_set::Green_function) against the reference's own G(z)
+    from its build_cf."""
+    g = load_golden(tag)
+    gcf = load_golden(tag + "_cf")
+    ns, nb, ops, params, sec = case_model(tag)
+    S, (up, dn, pr) = oracle_sector(tag)
+    L = ns + nb
+    al, be, e0 = qo.lanczos_eigenvalue(S.mult_add, g["h_x0"])
+    assert abs(e0 - gcf["gs_E0"]) < 1e-10 * abs(e0)
+    psi = qo.lanczos_eigenvector(S.mult_add, g["h_x0"], al, be)
+
+    def mao(nu, nd):
+        s = qo.Sector(L, nu, nd, up, dn, pr)
+        return s.mult_add, s.dim
+
+    af = CASES[tag][3]
+    for spin_down in ((False, True) if af else (False,)):
+        G = qo.cf_green_function_for_state(mao, L, S.nup, S.ndn, psi, e0, 1.0, list(range(ns)),
+                                           ZS, spin_down)
+        for k in range(len(ZS)):
+            ref = gcf[("gzdn" if spin_down else "gz") + str(k)]
+            assert np.max(np.abs(G[k] - ref)) < 1e-9, (tag, spin_down, k, np.max(np.abs(G[k] - ref)))
