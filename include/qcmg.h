@@ -203,6 +203,24 @@ int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_targe
 int qcmg_lanczos_green(qcmg_hamiltonian* H, const double* psi, unsigned flags, double accur,
                        int max_iter, int* n, double* a, double* b, int cap);
 
+/* Block Lanczos for the matrix continued fraction (GF_method 'M'), with
+ * the reference's default polar coupling blocks: p start vectors phi (p x
+ * dim, row-major; device pointers with QCMG_DEVICE_PTRS) are factored
+ * phi = q W by modified Gram-Schmidt (stopping at the first column of norm
+ * below acc_deflation: *p_actual <= p), then the block recurrence
+ * H Q_j = Q_{j-1} B_{j-1} + Q_j A_j + Q_{j+1} B_j runs for at most
+ * min(M_target, max_iter) steps, stopping when the lowest eigenvalue of the
+ * block-tridiagonal projection moves by less than acc_band between checks
+ * (every p_actual steps) or a coupling block becomes singular.
+ * Outputs: *M blocks A and B (each p_actual x p_actual, row-major, the last B
+ * being the truncation residual) and W (p_actual x p, row-major); capacity
+ * cap >= *M blocks.  Replaces blockLanczosSVD (src_ed/Hamiltonian/Lanczos.hpp:
+ * 603-790) and the start-block factorization of model_instance::build_mcf
+ * (src_ed/model_instance.hpp:847-955). */
+int qcmg_block_lanczos(qcmg_hamiltonian* H, int p, const double* phi, unsigned flags,
+                       int M_target, int max_iter, double acc_deflation, double acc_band, int* M,
+                       int* p_actual, double* A, double* B, double* W, int cap);
+
 /* qcmg_band_lanczos with the start vectors already in the handle's device
  * memory (p x dim, row-major; e.g. written there by qcmg_apply_c with
  * QCMG_DEVICE_PTRS), so they cross no host link.  The call waits for the

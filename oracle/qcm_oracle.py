@@ -493,3 +493,142 @@ def cf_green_function_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, weight, o
                 t = 0.5 * (part(i1, i2) - d[i1] - d[i2])
                 G[w, i1, i2] = G[w, i2, i1] = t
     return G
+
+
+# ----------------------------------------------------------------------------
+# Matrix continued-fraction Green function (GF_method 'M')
+
+
+def _lowest_banded(A, B, p):
+    """Lowest eigenvalue of the block-tridiagonal matrix with diagonal blocks
+    A[j] and sub-diagonal blocks B[j] (LAPACK band eigensolver)."""
+    from scipy.linalg import eigvals_banded
+    m = len(A)
+    sz = m * p
+    bw = 2 * p - 1
+    ab = np.zeros((bw + 1, sz))  # lower band: ab[r - c, c]
+    for jj in range(m):
+        for r in range(p):
+            for c in range(p):
+                if r >= c:
+                    ab[r - c, jj * p + c] = A[jj][r, c]
+                if jj < m - 1:
+                    ab[p + r - c, jj * p + c] = B[jj][r, c]
+    return float(eigvals_banded(ab, lower=True, select="i", select_range=(0, 0))[0])
+
+
+def block_lanczos_svd(mult_add, q, M0, accur_deflation=1e-7, accur_band=1e-12, max_iter_BL=600):
+    """(A, B) of the reference's blockLanczosSVD (Lanczos.hpp:603-790): the
+    block recurrence H Q_j = Q_{j-1} B_{j-1} + Q_j A_j + Q_{j+1} B_j with B_j
+    the symmetric square root of the residual's Gram matrix; convergence of
+    the lowest eigenvalue of the block-tridiagonal matrix every p steps from
+    step 2p, singular coupling blocks (eigenvalue of the Gram matrix below
+    accur_deflation^2) stop the recurrence."""
+    p = len(q)
+    M0 = min(M0, max_iter_BL)
+    Qc = [np.array(v, np.float64) for v in q]
+    for l in range(p):  # the block is orthonormalized once more
+        for k in range(l):
+            Qc[l] = Qc[l] - float(Qc[k] @ Qc[l]) * Qc[k]
+        nrm = float(np.linalg.norm(Qc[l]))
+        if nrm < accur_deflation:
+            raise RuntimeError("block Lanczos: rank-deficient start block")
+        Qc[l] = Qc[l] / nrm
+    Qp = None
+    A, B = [], []
+    ev_old = 1e12
+    for j in range(M0):
+        Z = []
+        for k in range(p):
+            z = np.zeros(len(Qc[k]))
+            mult_add(Qc[k], z)
+            Z.append(z)
+        Aj = np.array([[float(Qc[k] @ Z[l]) for l in range(p)] for k in range(p)])
+        Aj = np.triu(Aj) + np.triu(Aj, 1).T  # computed for k <= l, mirrored
+        A.append(Aj)
+        for l in range(p):
+            for k in range(p):
+                Z[l] = Z[l] - Aj[k, l] * Qc[k]
+        if j > 0:
+            Bp = B[-1]
+            for l in range(p):
+                for k in range(p):
+                    Z[l] = Z[l] - Bp[l, k] * Qp[k]
+        G = np.array([[float(Z[k] @ Z[l]) for l in range(p)] for k in range(p)])
+        G = np.triu(G) + np.triu(G, 1).T
+        D, V = np.linalg.eigh(G)
+        singular = bool(np.any(D < accur_deflation ** 2))
+        B.append((V * np.sqrt(np.maximum(D, 0.0))) @ V.T)
+        if singular:
+            break
+        Binv = (V / np.sqrt(D)) @ V.T
+        Qn = [sum(Binv[k, l] * Z[k] for k in range(p)) for l in range(p)]
+        Qp, Qc = Qc, Qn
+        if j + 1 >= 2 * p and (j + 1) % p == 0:
+            e0 = _lowest_banded(A, B, p)
+            delta = abs(e0 - ev_old)
+            ev_old = e0
+            if delta < accur_band:
+                break
+    return A, B
+
+
+def mcf_evaluate(A, B, W, z):
+    """G(z) = W^T F_0 W with F_M = 0, F_j = (z - A_j - B_j^T F_{j+1} B_j)^-1
+    (matrix_continued_fraction.hpp:139-185; the last B is not used)."""
+    p = A[0].shape[0]
+    F = np.zeros((p, p), np.complex128)
+    M = len(A)
+    for j in range(M - 1, -1, -1):
+        S = B[j].T @ F @ B[j] if j < M - 1 else 0.0
+        F = np.linalg.inv(z * np.eye(p) - A[j] - S)
+    return W.T @ F @ W
+
+
+def mcf_green_function_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, weight, orbitals, zs,
+                                 spin_down=False, accur_deflation=1e-7):
+    """G(z) of one ground state by matrix continued fractions, real case, as
+    model_instance::build_mcf (model_instance.hpp:847-955) and
+    mcf_set::Green_function (mcf_set.hpp:112-130) form it: per part
+    (pm = -1 holes, +1 electrons) the start block c_o psi, its Gram-Schmidt
+    factor W (times sqrt(weight)), block Lanczos on the orthonormal block, and
+    the shifted fraction; G = G_e + G_h^T.  Returns (nz, L, L)."""
+    spin = 1 if spin_down else 0
+    parts = []
+    for pm in (-1, 1):
+        nup2 = nup + (0 if spin else pm)
+        ndn2 = ndn + (pm if spin else 0)
+        if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L_orb:
+            continue
+        mult_add, dim = mult_add_of(nup2, ndn2)
+        if dim == 0:
+            continue
+        phi = [apply_c(L_orb, o + spin * L_orb, pm, nup, ndn, psi) for o in orbitals]
+        p = len(phi)
+        q = [v.copy() for v in phi]
+        W = np.zeros((p, p))
+        pa = p
+        for l in range(p):
+            for k in range(l):
+                z = float(q[k] @ q[l])
+                W[k, l] = z
+                q[l] = q[l] - z * q[k]
+            nrm = float(np.linalg.norm(q[l]))
+            if nrm < accur_deflation:
+                pa = l
+                break
+            W[l, l] = nrm
+            q[l] = q[l] / nrm
+        if pa == 0:
+            continue
+        W = W[:pa] * np.sqrt(weight)
+        A, B = block_lanczos_svd(mult_add, q[:pa], int(14 * pa * np.log(1.0 * dim)))
+        A = [a - E0 * np.eye(pa) if pm == 1 else E0 * np.eye(pa) - a for a in A]
+        parts.append((pm, A, B, W))
+    zs = np.atleast_1d(np.asarray(zs, np.complex128))
+    G = np.zeros((len(zs), len(orbitals), len(orbitals)), np.complex128)
+    for w, z in enumerate(zs):
+        for pm, A, B, W in parts:
+            g = mcf_evaluate(A, B, W, z)
+            G[w] += g if pm == 1 else g.T
+    return G

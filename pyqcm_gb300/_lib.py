@@ -62,6 +62,8 @@ SIGNATURES = {
     "qcmg_band_lanczos_device": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p,
                                          vp, vp, c_int]),
     "qcmg_lanczos_green": (c_int, [vp, vp, c_uint, c_double, c_int, int_p, vp, vp, c_int]),
+    "qcmg_block_lanczos": (c_int, [vp, c_int, vp, c_uint, c_int, c_int, c_double, c_double, int_p,
+                                   int_p, vp, vp, vp, c_int]),
     "qcmg_apply_c": (c_int, [c_int, c_int, c_int, c_int, c_int, vp, vp, c_double, c_uint]),
     "qcmg_green_function": (c_int, [c_int, c_int, vp, vp, c_int, vp, vp]),
     "qcmg_lattice_create": (c_int, [c_int, c_int, vp, c_int, vp, vp, vp, vp, vp, vp,

@@ -465,6 +465,30 @@ int qcmg_lanczos_green(qcmg_hamiltonian* H, const double* psi, unsigned flags, d
   });
 }
 
+int qcmg_block_lanczos(qcmg_hamiltonian* H, int p, const double* phi, unsigned flags,
+                       int M_target, int max_iter, double acc_deflation, double acc_band, int* M,
+                       int* p_actual, double* A, double* B, double* W, int cap) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && phi != nullptr && M != nullptr && p_actual != nullptr,
+                   "NULL argument");
+    QCMG_CHECK_ARG(p > 0 && M_target > 0 && max_iter > 0, "invalid block Lanczos sizes");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    *M = 0;
+    *p_actual = 0;
+    if (H->dim == 0) return;
+    const bool dev = (flags & QCMG_DEVICE_PTRS) != 0;
+    if (dev) QCMG_CUDA(cudaDeviceSynchronize());  // start vectors may come from any stream
+    BlockResult r = block_lanczos(H, p, phi, dev, M_target, max_iter, acc_deflation, acc_band);
+    QCMG_CHECK_ARG(r.M <= cap, "block Lanczos output capacity too small");
+    *M = r.M;
+    *p_actual = r.pa;
+    if (A) std::copy(r.A.begin(), r.A.end(), A);
+    if (B) std::copy(r.B.begin(), r.B.end(), B);
+    if (W) std::copy(r.W.begin(), r.W.end(), W);
+  });
+}
+
 static int band_lanczos_entry(qcmg_hamiltonian* H, int p, const double* phi, bool on_device,
                               int M_target, int max_iter, double acc_deflation, double acc_band,
                               int* M, double* evals, double* Q, int cap) {

@@ -584,6 +584,163 @@ GreenResult lanczos_green(qcmg_hamiltonian* H, const double* psi0, bool on_devic
   return out;
 }
 
+// Block Lanczos with Hermitian (polar) coupling blocks, the reference's
+// default block method for matrix continued fractions (blockLanczosSVD,
+// src_ed/Hamiltonian/Lanczos.hpp:603-790), preceded by the QR factor W of the
+// start vectors that build_mcf extracts (model_instance.hpp:884-915).  All
+// length-dim vectors stay on the device; the host holds the p x p blocks.
+BlockResult block_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool on_device,
+                          int M0, int max_iter, double acc_defl, double acc_band) {
+  const size_t n = H->dim;
+  cudaStream_t s = H->stream;
+  BlockResult out;
+  QCMG_CHECK_ARG(p > 0, "block Lanczos needs at least one start vector");
+  if (n == 0) return out;
+  Reducer red;
+  MultiOps mops;
+  std::vector<DevVec> store;
+  std::vector<double*> q(p);
+  for (int k = 0; k < p; ++k) {
+    store.emplace_back(n);
+    q[k] = store.back().p;
+    QCMG_CUDA(cudaMemcpyAsync(q[k], phi_in + (size_t)k * n, n * 8,
+                              on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  }
+  // modified Gram-Schmidt of the start block: phi[l] = sum_{k<=l} q[k] W(k,l);
+  // the block stops at the first column whose norm falls below acc_defl
+  std::vector<double> W((size_t)p * p, 0.0);
+  int pa = p;
+  for (int l = 0; l < p; ++l) {
+    for (int k = 0; k < l; ++k) {
+      const double z = red.dot(q[k], q[l], n, s);
+      W[(size_t)k * p + l] = z;
+      axpy(q[l], q[k], -z, n, s);
+    }
+    const double nrm = std::sqrt(red.dot(q[l], q[l], n, s));
+    if (nrm < acc_defl) {
+      pa = l;
+      break;
+    }
+    W[(size_t)l * p + l] = nrm;
+    scale(q[l], 1.0 / nrm, n, s);
+  }
+  out.pa = pa;
+  out.W.assign(W.begin(), W.begin() + (size_t)pa * p);
+  if (pa == 0) return out;
+  // build_mcf sizes the run on the block that survives: 14 p' ln(dim)
+  if (pa < p) M0 = (int)(14 * pa * std::log(1.0 * n));
+  // blockLanczosSVD orthonormalizes the (already orthonormal) block once more
+  for (int l = 0; l < pa; ++l) {
+    for (int k = 0; k < l; ++k) axpy(q[l], q[k], -red.dot(q[k], q[l], n, s), n, s);
+    const double nrm = std::sqrt(red.dot(q[l], q[l], n, s));
+    if (nrm < acc_defl) throw Error(QCMG_ERR_NUMERIC, "block Lanczos: rank-deficient start block");
+    scale(q[l], 1.0 / nrm, n, s);
+  }
+  if (M0 > max_iter) M0 = max_iter;
+  // four blocks of pa vectors: Q_prev, Q_cur, Z, Q_next (rotated by pointer)
+  auto block = [&]() {
+    std::vector<double*> b(pa);
+    for (int k = 0; k < pa; ++k) {
+      store.emplace_back(n);
+      b[k] = store.back().p;
+    }
+    return b;
+  };
+  std::vector<double*> Qc(q.begin(), q.begin() + pa), Qp = block(), Z = block(), Qn = block();
+  const int pp = pa * pa;
+  std::vector<double> Aj(pp), Bj(pp), G(pp), Binv(pp), D, V, dots, col(pa);
+  std::vector<const double*> lst;
+  std::vector<double> t;  // block-tridiagonal T, column-major, for the convergence probe
+  double ev_old = 1e12, last_change = INFINITY;
+  for (int j = 0; j < M0; ++j) {
+    for (int k = 0; k < pa; ++k) matvec(H, Qc[k], Z[k], false);  // Z = H Q
+    // A(k,l) = <Q_k|Z_l>, k <= l, mirrored
+    for (int l = 0; l < pa; ++l) {
+      lst.assign(Qc.begin(), Qc.begin() + l + 1);
+      mops.multidot(lst, Z[l], n, s, dots);
+      for (int k = 0; k <= l; ++k) Aj[(size_t)k * pa + l] = Aj[(size_t)l * pa + k] = dots[k];
+    }
+    out.A.insert(out.A.end(), Aj.begin(), Aj.end());
+    // Z_l -= sum_k A(k,l) Q_k  (- sum_k B_{j-1}(l,k) Qprev_k for j > 0)
+    for (int l = 0; l < pa; ++l) {
+      lst.assign(Qc.begin(), Qc.end());
+      for (int k = 0; k < pa; ++k) col[k] = Aj[(size_t)k * pa + l];
+      if (j > 0) {
+        lst.insert(lst.end(), Qp.begin(), Qp.end());
+        for (int k = 0; k < pa; ++k) col.push_back(out.B[(size_t)(j - 1) * pp + (size_t)l * pa + k]);
+      }
+      mops.multiaxpy(lst, col, Z[l], n, s);
+      col.resize(pa);
+    }
+    // polar decomposition of Z: Gram G = V D V^T, B_j = V D^1/2 V^T
+    for (int l = 0; l < pa; ++l) {
+      lst.assign(Z.begin(), Z.begin() + l + 1);
+      mops.multidot(lst, Z[l], n, s, dots);
+      for (int k = 0; k <= l; ++k) G[(size_t)k * pa + l] = G[(size_t)l * pa + k] = dots[k];
+    }
+    std::vector<double> gcm((size_t)pa * pa);  // lower triangle, column-major, for the solver
+    for (int c = 0; c < pa; ++c)
+      for (int r = 0; r < pa; ++r) gcm[(size_t)r + (size_t)pa * c] = G[(size_t)r * pa + c];
+    if (!band_eigen_leading(gcm, pa, pa, pa - 1, pa, D, V))  // V[k*pa + m]: component k of vector m
+      throw Error(QCMG_ERR_NUMERIC, "block Lanczos: Gram eigensolver did not converge");
+    bool singular = false;
+    for (int m = 0; m < pa; ++m)
+      if (D[m] < acc_defl * acc_defl) {
+        singular = true;
+        break;
+      }
+    for (int r = 0; r < pa; ++r)
+      for (int c = 0; c < pa; ++c) {
+        double b = 0.0, bi = 0.0;
+        for (int m = 0; m < pa; ++m) {
+          const double vv = V[(size_t)r * pa + m] * V[(size_t)c * pa + m];
+          b += vv * std::sqrt(std::max(D[m], 0.0));
+          if (!singular) bi += vv / std::sqrt(D[m]);
+        }
+        Bj[(size_t)r * pa + c] = b;
+        Binv[(size_t)r * pa + c] = bi;
+      }
+    out.B.insert(out.B.end(), Bj.begin(), Bj.end());
+    out.M = j + 1;
+    if (singular) break;
+    // Q_next_l = sum_k Binv(k,l) Z_k  (into zeroed vectors: w -= sum (-c) V)
+    for (int l = 0; l < pa; ++l) {
+      QCMG_CUDA(cudaMemsetAsync(Qn[l], 0, n * 8, s));
+      lst.assign(Z.begin(), Z.end());
+      for (int k = 0; k < pa; ++k) col[k] = -Binv[(size_t)k * pa + l];
+      mops.multiaxpy(lst, col, Qn[l], n, s);
+    }
+    std::swap(Qp, Qc);  // Q_prev <- Q_cur
+    std::swap(Qc, Qn);  // Q_cur <- Q_next (the old Q_prev becomes scratch)
+    // convergence every pa steps: lowest eigenvalue of the block-tridiagonal
+    // projection (half bandwidth 2 pa - 1, so the banded probe applies)
+    if ((j + 1) >= 2 * pa && (j + 1) % pa == 0) {
+      const int sz = (j + 1) * pa, bw = 2 * pa - 1;
+      t.assign((size_t)(bw + 1) * sz, 0.0);  // packed lower band: (r, c) at (r - c) + (bw + 1) c
+      auto put = [&](int r, int c, double v) {
+        if (r >= c) t[(size_t)(r - c) + (size_t)(bw + 1) * c] = v;
+      };
+      for (int jj = 0; jj <= j; ++jj)
+        for (int r = 0; r < pa; ++r)
+          for (int c = 0; c < pa; ++c) {
+            put(jj * pa + r, jj * pa + c, out.A[(size_t)jj * pp + r * pa + c]);
+            if (jj < j) put((jj + 1) * pa + r, jj * pa + c, out.B[(size_t)jj * pp + r * pa + c]);
+          }
+      const bool warm = ev_old < 1e12;
+      const double width = std::isfinite(last_change) && warm
+                               ? std::max(4.0 * last_change, 1e-12 * std::max(1.0, std::fabs(ev_old)))
+                               : 1e-3 * std::max(1.0, std::fabs(ev_old));
+      const double e0 = warm ? band_lowest_packed(t, sz, bw, ev_old, width)
+                             : band_lowest_packed(t, sz, bw);
+      const double delta = std::fabs(e0 - ev_old);
+      if (ev_old < 1e12) last_change = delta;
+      ev_old = e0;
+      if (delta < acc_band) break;
+    }
+  }
+  return out;
+}
+
 BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device, int M0,
                         int max_iter,
                         double acc_defl, double acc_band) {

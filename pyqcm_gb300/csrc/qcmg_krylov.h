@@ -38,6 +38,17 @@ struct GreenResult {
 GreenResult lanczos_green(qcmg_hamiltonian* H, const double* psi0, bool on_device, double accur,
                           int max_iter);
 
+struct BlockResult {
+  int M = 0;              // block steps
+  int pa = 0;             // block size after the start block's deflation
+  std::vector<double> A;  // M blocks pa x pa, row-major
+  std::vector<double> B;  // M blocks pa x pa (the last one is the truncation residual)
+  std::vector<double> W;  // pa x p, row-major: phi = q W
+};
+
+BlockResult block_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool on_device,
+                          int M0, int max_iter, double acc_defl, double acc_band);
+
 // phi_in: p start vectors of length dim, vector k at phi_in + k*dim, in
 // host memory or (phi_on_device) in the handle's device memory.
 BandResult band_lanczos(qcmg_hamiltonian* H, int p, const double* phi_in, bool phi_on_device,

@@ -79,16 +79,20 @@ double tridiag_lowest(const std::vector<double>& a, const std::vector<double>& b
   return lam;
 }
 
+// The band solvers read the matrix through low(r, c), the element (r, c)
+// for r >= c within the band: the leading block of a dense column-major
+// array, or packed band storage.
+
 // True when A - sigma I is positive definite; A is the leading n x n block
 // of the band matrix, L (n x (b+1), row i holds L(i, i-b..i)) is scratch.
-static bool band_posdef(const std::vector<double>& t, int ld, int n, int b, double sigma,
-                        std::vector<double>& L) {
+template <class Low>
+static bool band_posdef(const Low& low, int n, int b, double sigma, std::vector<double>& L) {
   const int w = b + 1;
   auto Lr = [&](int i, int k) -> double& { return L[(size_t)i * w + (k - i + b)]; };
   for (int i = 0; i < n; ++i) {
     const int k0 = std::max(0, i - b);
     for (int k = k0; k <= i; ++k) {
-      double s = t[(size_t)i + (size_t)ld * k] - (k == i ? sigma : 0.0);
+      double s = low(i, k) - (k == i ? sigma : 0.0);
       for (int m = std::max(k0, k - b); m < k; ++m) s -= Lr(i, m) * Lr(k, m);
       if (k < i) {
         Lr(i, k) = s / Lr(k, k);
@@ -104,13 +108,11 @@ static bool band_posdef(const std::vector<double>& t, int ld, int n, int b, doub
 // Inverse iteration with the Cholesky factor L of A - sigma I (sigma below
 // the lowest eigenvalue), then the Rayleigh quotient of the iterate: the
 // lowest eigenvalue when the iteration has converged.  O(n b) per step.
-static bool band_refine(const std::vector<double>& t, int ld, int n, int b,
-                        const std::vector<double>& L, double* lam) {
+template <class Low>
+static bool band_refine(const Low& low, int n, int b, const std::vector<double>& L, double* lam) {
   const int w = b + 1;
   auto Lr = [&](int i, int k) { return L[(size_t)i * w + (k - i + b)]; };
-  auto A = [&](int r, int c) {
-    return r >= c ? t[(size_t)r + (size_t)ld * c] : t[(size_t)c + (size_t)ld * r];
-  };
+  auto A = [&](int r, int c) { return r >= c ? low(r, c) : low(c, r); };
   std::vector<double> x(n), y(n);
   for (int i = 0; i < n; ++i) x[i] = 1.0 + 0.25 * std::sin(0.7 * i + 0.3);
   for (int it = 0; it < 8; ++it) {
@@ -140,11 +142,11 @@ static bool band_refine(const std::vector<double>& t, int ld, int n, int b,
   return std::isfinite(q);
 }
 
-double band_lowest(const std::vector<double>& t, int ld, int n, int b, double near,
-                   double width) {
+template <class Low>
+static double band_lowest_impl(const Low& low, int n, int b, double near, double width) {
   if (n <= 0) return 0.0;
   b = std::max(0, std::min(b, n - 1));
-  auto A = [&](int r, int c) { return r >= c ? t[(size_t)r + (size_t)ld * c] : t[(size_t)c + (size_t)ld * r]; };
+  auto A = [&](int r, int c) { return r >= c ? low(r, c) : low(c, r); };
   // lambda_min <= min_i A(i,i); Gershgorin gives the lower end.
   double glo = INFINITY, hi = INFINITY, scale = 0.0;
   for (int i = 0; i < n; ++i) {
@@ -162,11 +164,11 @@ double band_lowest(const std::vector<double>& t, int ld, int n, int b, double ne
     // start from a bracket below the hint and widen it until A - lo I is
     // definite (the Gershgorin end always is)
     const double top = near + 64.0 * DBL_EPSILON * std::max(scale, 1.0);
-    if (top < hi && !band_posdef(t, ld, n, b, top, L)) hi = top;
+    if (top < hi && !band_posdef(low, n, b, top, L)) hi = top;
     for (double w = width;; w *= 8.0) {
       const double cand = hi - w;
       if (cand <= glo) break;
-      if (band_posdef(t, ld, n, b, cand, L)) {
+      if (band_posdef(low, n, b, cand, L)) {
         lo = cand;
         break;
       }
@@ -185,20 +187,33 @@ double band_lowest(const std::vector<double>& t, int ld, int n, int b, double ne
     if (!tried && hi - lo <= refine_at) {
       tried = true;
       double lam;
-      if (band_posdef(t, ld, n, b, lo, L) && band_refine(t, ld, n, b, L, &lam) &&
+      if (band_posdef(low, n, b, lo, L) && band_refine(low, n, b, L, &lam) &&
           lam - eta > lo && lam + eta < hi) {
-        if (band_posdef(t, ld, n, b, lam - eta, L) && !band_posdef(t, ld, n, b, lam + eta, L))
+        if (band_posdef(low, n, b, lam - eta, L) && !band_posdef(low, n, b, lam + eta, L))
           return lam;
       }
     }
     const double mid = 0.5 * (lo + hi);
     if (mid <= lo || mid >= hi) break;
-    if (band_posdef(t, ld, n, b, mid, L))
+    if (band_posdef(low, n, b, mid, L))
       lo = mid;
     else
       hi = mid;
   }
   return 0.5 * (lo + hi);
+}
+
+double band_lowest(const std::vector<double>& t, int ld, int n, int b, double near,
+                   double width) {
+  auto low = [&](int r, int c) { return t[(size_t)r + (size_t)ld * c]; };
+  return band_lowest_impl(low, n, b, near, width);
+}
+
+double band_lowest_packed(const std::vector<double>& ab, int n, int b, double near,
+                          double width) {
+  const size_t w = (size_t)b + 1;
+  auto low = [&](int r, int c) { return ab[(size_t)(r - c) + w * c]; };
+  return band_lowest_impl(low, n, b, near, width);
 }
 
 namespace {

@@ -35,6 +35,12 @@ double tridiag_lowest(const std::vector<double>& alpha, const std::vector<double
 double band_lowest(const std::vector<double>& t, int ld, int n, int b, double near = NAN,
                    double width = 0.0);
 
+// band_lowest on packed band storage: element (r, c), r >= c, r - c <= b, at
+// ab[(r - c) + (b + 1) c] (the lower band of LAPACK's band layout), for
+// matrices too large to hold densely.
+double band_lowest_packed(const std::vector<double>& ab, int n, int b, double near = NAN,
+                          double width = 0.0);
+
 // All eigenvalues (ascending) of the same band matrix, and the leading p
 // rows of its eigenvectors: W[k * n + c] is component k of eigenvector c.
 // Band Lanczos needs no more to form its Q-matrix (Q = P U(0:p, :),

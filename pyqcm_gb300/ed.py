@@ -35,7 +35,8 @@ GLOBAL = {
     "seed": 0,
     "Lanczos_reorth": 0,
     # Green-function representation: 'L' Lehmann form from band Lanczos, 'F'
-    # continued fractions (src_util/global_parameter.cpp:61,76,90)
+    # continued fractions, 'M' matrix continued fractions (block Lanczos)
+    # (src_util/global_parameter.cpp:61,76,90)
     "GF_method": "L",
     "accur_continued_fraction": 0.01,
     "max_iter_CF": 400,
@@ -265,6 +266,27 @@ class Hamiltonian:
         m = n.value
         return a[:m].copy(), b[: m + 1].copy()
 
+    def block_lanczos(self, phi):
+        """Block Lanczos of the start block phi (p, dim) (host array or device
+        tensor): (A, B, W) with A, B lists of p' x p' blocks and W (p', p) the
+        start block's Gram-Schmidt factor (qcmg_block_lanczos)."""
+        p = int(phi.shape[0])
+        M = max(int(14 * p * math.log(1.0 * self.dim)), 1) if self.dim else 1
+        cap = GLOBAL["max_iter_BL"] + 1
+        A, B, W = np.zeros(cap * p * p), np.zeros(cap * p * p), np.zeros(p * p)
+        Mo, pa = _lib.c_int(), _lib.c_int()
+        if hasattr(phi, "data_ptr"):
+            src, flags = phi.data_ptr(), _lib.QCMG_DEVICE_PTRS
+        else:
+            phi = np.ascontiguousarray(phi, np.float64)
+            src, flags = ptr(phi), 0
+        check(lib().qcmg_block_lanczos(self._h, p, src, flags, M, GLOBAL["max_iter_BL"],
+                                       GLOBAL["accur_deflation"], GLOBAL["accur_band_lanczos"],
+                                       Mo, pa, ptr(A), ptr(B), ptr(W), cap))
+        m, q = Mo.value, pa.value
+        blocks = lambda X: [X[k * q * q:(k + 1) * q * q].reshape(q, q).copy() for k in range(m)]
+        return blocks(A), blocks(B), W[:q * p].reshape(q, p).copy()
+
     def build_Q_matrix(self, phi):
         """(e, Q) with Q of shape (p, M) (Hamiltonian_base.hpp:229-254)."""
         p = len(phi)
@@ -416,8 +438,9 @@ class ModelInstance:
         self.E0 = None
         self._H = {}
         self.gf_method = GLOBAL["GF_method"]
-        if self.gf_method not in ("L", "F"):
-            raise ValueError("GF_method must be 'L' (band Lanczos) or 'F' (continued fractions)")
+        if self.gf_method not in ("L", "F", "M"):
+            raise ValueError("GF_method must be 'L' (band Lanczos), 'F' (continued fractions) "
+                             "or 'M' (matrix continued fractions)")
 
     def hamiltonian(self, nup, ndn):
         key = (nup, ndn)
@@ -519,7 +542,7 @@ class ModelInstance:
         if self.gf_solved:
             return
         self.ground_state()
-        solve = self._cf_state if self.gf_method == "F" else self._qmatrix_state
+        solve = {"F": self._cf_state, "M": self._mcf_state}.get(self.gf_method, self._qmatrix_state)
         for st in self.states:
             st.gf = solve(st, False)
             if self.mixing & 4:
@@ -561,6 +584,58 @@ class ModelInstance:
                     a = a - st.energy if pm == 1 else st.energy - a
                     frac[(pm, o1, o2)] = (a, b)
         return frac
+
+    def _mcf_state(self, st, spin_down):
+        """Matrix continued fractions of one state, as model_instance::build_mcf
+        (model_instance.hpp:847-955): per part (pm = -1 holes, +1 electrons)
+        the start block c_o psi for all cluster orbitals, factored phi = q W
+        with W scaled by sqrt(weight), block Lanczos on q (polar coupling
+        blocks), and the diagonal blocks shifted by the energy.  Returns a
+        list of (pm, A, B, W)."""
+        L, ns = self.model.n_orb, self.model.n_sites
+        spin = 1 if spin_down else 0
+        parts = []
+        for pm in (-1, 1):
+            nup2 = st.sec.nup + (0 if spin else pm)
+            ndn2 = st.sec.ndn + (pm if spin else 0)
+            if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
+                continue
+            H = self.hamiltonian(nup2, ndn2)
+            if H.dim == 0:
+                continue
+            orbs = [o + spin * L for o in range(ns)]
+            if _cuda_ready():
+                phi = apply_c_device(L, orbs, pm, st.sec.nup, st.sec.ndn, self._psi_device(st))
+            else:
+                phi = np.array([apply_c(L, o, pm, st.sec.nup, st.sec.ndn, st.psi) for o in orbs])
+            A, B, W = H.block_lanczos(phi)
+            if not A:
+                continue
+            pa = A[0].shape[0]
+            eye = np.eye(pa)
+            A = [a - st.energy * eye if pm == 1 else st.energy * eye - a for a in A]
+            parts.append((pm, A, B, W * math.sqrt(st.weight)))
+        return parts
+
+    @staticmethod
+    def _mcf_green(parts, zs):
+        """G(z) (nz, L, L) of one state's matrix continued fractions: each part
+        W^T F_0(z) W with F_M = 0, F_j = (z - A_j - B_j^T F_{j+1} B_j)^-1
+        (matrix_continued_fraction.hpp:139-185), the hole part transposed
+        (mcf_set.hpp:112-130)."""
+        G = None
+        for pm, A, B, W in parts:
+            pa = A[0].shape[0]
+            eye = np.eye(pa)[None]
+            F = np.zeros((len(zs), pa, pa), np.complex128)
+            for j in range(len(A) - 1, -1, -1):
+                S = B[j].T[None] @ F @ B[j][None] if j < len(A) - 1 else 0.0
+                F = np.linalg.inv(zs[:, None, None] * eye - A[j][None] - S)
+            g = W.T[None] @ F @ W[None]
+            if pm == -1:
+                g = g.transpose(0, 2, 1)
+            G = g if G is None else G + g
+        return G
 
     def _cf_green(self, frac, zs):
         """G(z) (nz, L, L) of one state's continued fractions
@@ -610,7 +685,12 @@ class ModelInstance:
         G = None
         for st in self.states:
             gf = st.gf_down if (spin_down and self.mixing & 4) else st.gf
-            g = self._cf_green(gf, zs) if self.gf_method == "F" else green_function(*gf, zs)
+            if self.gf_method == "F":
+                g = self._cf_green(gf, zs)
+            elif self.gf_method == "M":
+                g = self._mcf_green(gf, zs)
+            else:
+                g = green_function(*gf, zs)
             G = g if G is None else G + g
         return G[0] if np.ndim(z) == 0 else G
 

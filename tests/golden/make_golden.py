@@ -87,10 +87,13 @@ def ed_case(tag, nx, ny, params, sector, n_bath=0, af=False, extra=(), gf=True, 
 CF_CASES = ["chain8", "ladder2x4_af", "plaquette_bath4"]
 
 
-def cf_case(tag):
+def cf_case(tag, method="F"):
+    """G(z) with GF_method F (continued fractions; sparse format, see above) or
+    M (matrix continued fractions from block Lanczos; factorized format)."""
     nx, ny, nb, af, params, sec, _ = CASES[tag]
     ns, nb, ops = hubbard_cluster(nx, ny, nb, af)
-    lines = ["gchar Hamiltonian_format S", "gchar GF_method F", "gint seed 0"]
+    fmt = "S" if method == "F" else "F"
+    lines = [f"gchar Hamiltonian_format {fmt}", f"gchar GF_method {method}", "gint seed 0"]
     lines += model_lines("clus", ns, nb, ops)
     lines += [f"param {k} {v!r}" for k, v in params.items() if k in ops]
     lines += [f"instance clus {sec} 1"]
@@ -100,16 +103,18 @@ def cf_case(tag):
             lines += [f"gz 1 1 {z.real!r} {z.imag!r} gzdn{k}"]
     lines += ["gs 1 gs"]
     out = run_spec(lines)
-    np.savez_compressed(os.path.join(HERE, tag + "_cf.npz"), **out)
-    print(tag + "_cf", sorted(k for k in out if k != "spec"))
+    suffix = "_cf" if method == "F" else "_mcf"
+    np.savez_compressed(os.path.join(HERE, tag + suffix + ".npz"), **out)
+    print(tag + suffix, sorted(k for k in out if k != "spec"))
 
 
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference oracle first: make -C oracle/refbuild")
-    if sys.argv[1:] == ["cf"]:  # the continued-fraction cases only
+    if sys.argv[1:] == ["cf"]:  # the (matrix) continued-fraction cases only
         for tag in CF_CASES:
             cf_case(tag)
+            cf_case(tag, "M")
         return
     # Half bases for L = 8, 12, 16 at half filling and one off-half filling.
     lines = ["halfbasis 8 4", "halfbasis 8 3", "halfbasis 12 6", "halfbasis 12 5", "halfbasis 16 8"]
@@ -125,6 +130,7 @@ def main():
         lattice_case(tag, c)
     for tag in CF_CASES:
         cf_case(tag)
+        cf_case(tag, "M")
 
 def lattice_case(tag, c):
     """Runs a lattice model through the reference's QCM layer."""

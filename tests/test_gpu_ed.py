@@ -153,14 +153,17 @@ def test_green_function_pipeline(pg, tag):
             assert np.max(np.abs(inst.self_energy(z) - g[f"sig{k}"])) < 1e-7
 
 
+@pytest.mark.parametrize("method", ["F", "M"])
 @pytest.mark.parametrize("tag", ["chain8", "ladder2x4_af", "plaquette_bath4"])
-def test_continued_fraction_green_function(pg, tag):
+def test_continued_fraction_green_function(pg, tag, method):
     """GF_method 'F': ground state -> c/c^dagger per orbital pair ->
-    continued-fraction Lanczos on the GPU -> G(z), against the reference's
-    own continued-fraction G(z) (build_cf, continued_fraction_set)."""
-    g = load_golden(tag + "_cf")
+    continued-fraction Lanczos on the GPU -> G(z); GF_method 'M': the start
+    block of all orbitals -> block Lanczos on the GPU -> matrix continued
+    fraction.  Both against the reference's own G(z) from build_cf /
+    build_mcf."""
+    g = load_golden(tag + ("_cf" if method == "F" else "_mcf"))
     m, params, sec = engine_model(tag)
-    pg.set_global_parameter("GF_method", "F")
+    pg.set_global_parameter("GF_method", method)
     try:
         inst = pg.ModelInstance(m, params, sec)
     finally:

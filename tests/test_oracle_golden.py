@@ -147,3 +147,30 @@ def test_continued_fraction_green_function_against_reference(tag):
         for k in range(len(ZS)):
             ref = gcf[("gzdn" if spin_down else "gz") + str(k)]
             assert np.max(np.abs(G[k] - ref)) < 1e-9, (tag, spin_down, k, np.max(np.abs(G[k] - ref)))
+
+
+@pytest.mark.parametrize("tag", ["chain8", "ladder2x4_af", "plaquette_bath4"])
+def test_matrix_continued_fraction_green_function_against_reference(tag):
+    """The oracle's restatement of the matrix continued fraction (GF_method
+    'M': start-block factor, blockLanczosSVD, matrix_continued_fraction,
+    mcf_set) against the reference's own G(z) from its build_mcf."""
+    g = load_golden(tag)
+    gm = load_golden(tag + "_mcf")
+    ns, nb, ops, params, sec = case_model(tag)
+    S, (up, dn, pr) = oracle_sector(tag)
+    L = ns + nb
+    al, be, e0 = qo.lanczos_eigenvalue(S.mult_add, g["h_x0"])
+    assert abs(e0 - gm["gs_E0"]) < 1e-10 * abs(e0)
+    psi = qo.lanczos_eigenvector(S.mult_add, g["h_x0"], al, be)
+
+    def mao(nu, nd):
+        s = qo.Sector(L, nu, nd, up, dn, pr)
+        return s.mult_add, s.dim
+
+    af = CASES[tag][3]
+    for spin_down in ((False, True) if af else (False,)):
+        G = qo.mcf_green_function_for_state(mao, L, S.nup, S.ndn, psi, e0, 1.0, list(range(ns)),
+                                            ZS, spin_down)
+        for k in range(len(ZS)):
+            ref = gm[("gzdn" if spin_down else "gz") + str(k)]
+            assert np.max(np.abs(G[k] - ref)) < 1e-10, (tag, spin_down, k, np.max(np.abs(G[k] - ref)))
