@@ -294,6 +294,15 @@ int qcmg_sef_grid(qcmg_lattice* lat, int nw, const double* w, const double* wt, 
 int qcmg_cpt_periodized(qcmg_lattice* lat, int nz, const double* z, int nk, const double* K,
                         double* g);
 
+/* Mean of the CPT Green function (G(z)^-1 - V(K))^-1 over the K grid
+ * ((i + off)/nkx, (j + off)/nky, (l + off)/nkz) for nz complex frequencies z
+ * (re, im pairs); out is nz blocks of L x L complex, row-major.  Replaces
+ * the K sums of lattice_model_instance::dos on the wavevector grid
+ * (src_qcm/average.cpp:294-347, whose diagonal gives the density of states)
+ * and of projected_Green_function. */
+int qcmg_lattice_kmean(qcmg_lattice* lat, int nz, const double* z, int nkx, int nky, int nkz,
+                       double off, double* out);
+
 /* Projected (k-averaged) CPT Green function on the midpoint grid of side
  * kside in dimk dimensions, at imaginary frequencies i w: pgf is nw blocks of
  * L x L complex, row-major.  Replaces lattice_model_instance::

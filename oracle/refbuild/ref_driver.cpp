@@ -32,6 +32,7 @@
 //   lat_kgrid NX NY NZ                        -> QCM::set_wavevector_grid
 //   lat_wgrid N w_1..w_N p_1..p_N             -> discrete frequency grid
 //   lat_sef LABEL TAG                         -> QCM::Potthoff_functional
+//   lat_dos LABEL TAG NZ (re im)x NZ          -> QCM::dos on the wavevector grid
 //   lat_gper LABEL TAG NZ (re im)x NZ NK (kx ky kz)x NK -> periodized_Green_function
 //   lat_tk LABEL TAG NK (kx ky kz)x NK        -> QCM::tk
 //   lat_dump LABEL TAG                        -> neighbours, inter-cluster elements, H, Hc
@@ -332,6 +333,19 @@ int main(int argc, char** argv) {
       } else if (cmd == "lat_sef") {
         int label; string tag; ss >> label >> tag;
         put_scalar(tag, QCM::Potthoff_functional(label));
+      } else if (cmd == "lat_dos") {
+        // lat_dos LABEL TAG NZ (re im)x NZ: QCM::dos on the wavevector grid,
+        // one row of 2 n_band values per frequency
+        int label, nz; string tag; ss >> label >> tag >> nz;
+        vector<double> all;
+        size_t width = 0;
+        for (int i = 0; i < nz; i++) {
+          double re, im; ss >> re >> im;
+          vector<double> d = QCM::dos(cplx(re, im), label, true);
+          width = d.size();
+          all.insert(all.end(), d.begin(), d.end());
+        }
+        put(tag, "f8", {(size_t)nz, width}, all.data(), all.size());
       } else if (cmd == "lat_gper" || cmd == "lat_tk") {
         int label; string tag; ss >> label >> tag;
         vector<cplx> zs;

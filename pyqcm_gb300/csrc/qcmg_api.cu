@@ -700,6 +700,18 @@ int qcmg_cpt_periodized(qcmg_lattice* h, int nz, const double* z, int nk, const 
   });
 }
 
+int qcmg_lattice_kmean(qcmg_lattice* h, int nz, const double* z, int nkx, int nky, int nkz,
+                       double off, double* out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h && z && out, "NULL argument");
+    QCMG_CHECK_ARG(nz > 0 && nkx > 0 && nky > 0 && nkz > 0, "invalid sizes");
+    std::lock_guard<std::mutex> lock(h->mu);
+    QCMG_CHECK_ARG(h->lat.M >= 0, "the Green function was not set");
+    QCMG_CUDA(cudaSetDevice(h->lat.device));
+    h->lat.kmean(nz, z, nkx, nky, nkz, off, out, h->lat.stream);
+  });
+}
+
 int qcmg_cdmft_projected(qcmg_lattice* h, int nw, const double* w, int kside, int dimk,
                          double* pgf) {
   return guarded([&] {

@@ -521,32 +521,44 @@ void Lattice::projected(int nw, const double* w, int kside, int dimk, double* pg
     z[2 * i] = 0.0;
     z[2 * i + 1] = w[i];
   }
-  prepare(nw, z.data(), s);
-  PointArgs A = point_args(*this, nw);
-  int nk = 1;
-  A.gx = dimk >= 1 ? kside : 1;
-  A.gy = dimk >= 2 ? kside : 1;
-  A.gz = dimk >= 3 ? kside : 1;
-  nk = A.gx * A.gy * A.gz;
-  A.nk = nk;
-  A.off = dimk >= 1 ? 0.5 : 0.0;
-  A.tab = (const double2*)phase_tables(A.gx, A.gy, A.gz, A.off, s);
-  const int LL = L * L;
-  DevBuf<double> inv, out;
-  inv.alloc((size_t)2 * nw * nk * LL);
-  out.alloc((size_t)2 * nw * LL);
-  A.out = (double2*)inv.p;
+  const int g = kside;
+  kmean(nw, z.data(), dimk >= 1 ? g : 1, dimk >= 2 ? g : 1, dimk >= 3 ? g : 1,
+        dimk >= 1 ? 0.5 : 0.0, pgf, s);
+}
+
+void Lattice::kmean(int nz, const double* z, int gx, int gy, int gz, double off, double* out_host,
+                    cudaStream_t s) {
+  const int nk = gx * gy * gz, LL = L * L;
   const int T = point_threads(L);
   const size_t smem = (size_t)2 * L * L * T * 8;
   QCMG_CUDA(cudaFuncSetAttribute(k_points<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  const size_t npts = (size_t)nw * nk;
-  unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
-  k_points<2><<<gr, T, smem, s>>>(A);
-  k_mean_inverse<<<(nw * LL + 255) / 256, 256, 0, s>>>((const double2*)inv.p, nw, nk, LL,
-                                                       (double2*)out.p);
-  QCMG_CUDA(cudaGetLastError());
-  QCMG_CUDA(cudaMemcpyAsync(pgf, out.p, (size_t)2 * nw * LL * 8, cudaMemcpyDeviceToHost, s));
-  QCMG_CUDA(cudaStreamSynchronize(s));
+  // frequencies in chunks whose per-point inverses fit in ~512 MB
+  const size_t per_z = (size_t)nk * LL * 16;
+  const int chunk = (int)std::max<size_t>(1, std::min<size_t>(nz, ((size_t)512 << 20) / per_z));
+  DevBuf<double> inv, out;
+  inv.alloc((size_t)2 * chunk * nk * LL);
+  out.alloc((size_t)2 * chunk * LL);
+  for (int z0 = 0; z0 < nz; z0 += chunk) {
+    const int nc = std::min(chunk, nz - z0);
+    prepare(nc, z + 2 * (size_t)z0, s);
+    PointArgs A = point_args(*this, nc);
+    A.gx = gx;
+    A.gy = gy;
+    A.gz = gz;
+    A.nk = nk;
+    A.off = off;
+    A.tab = (const double2*)phase_tables(gx, gy, gz, off, s);
+    A.out = (double2*)inv.p;
+    const size_t npts = (size_t)nc * nk;
+    unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
+    k_points<2><<<gr, T, smem, s>>>(A);
+    k_mean_inverse<<<(nc * LL + 255) / 256, 256, 0, s>>>((const double2*)inv.p, nc, nk, LL,
+                                                         (double2*)out.p);
+    QCMG_CUDA(cudaGetLastError());
+    QCMG_CUDA(cudaMemcpyAsync(out_host + (size_t)2 * z0 * LL, out.p, (size_t)2 * nc * LL * 8,
+                              cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaStreamSynchronize(s));
+  }
 }
 
 }  // namespace qcmg

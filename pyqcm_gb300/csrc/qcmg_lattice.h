@@ -40,6 +40,11 @@ struct Lattice {
                   cudaStream_t s);
   void cpt(int nz, const double* z, int nk, const double* K, double* g, cudaStream_t s);
   void projected(int nw, const double* w, int kside, int dimk, double* pgf, cudaStream_t s);
+  // mean over the K grid ((i + off)/gx, ...) of the CPT Green function
+  // (G(z)^-1 - V(K))^-1, for nz complex frequencies z (re, im pairs);
+  // out: nz x L x L complex, row-major
+  void kmean(int nz, const double* z, int gx, int gy, int gz, double off, double* out,
+             cudaStream_t s);
 };
 
 }  // namespace qcmg

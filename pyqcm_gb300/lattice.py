@@ -334,6 +334,31 @@ class LatticeInstance:
         z = np.asarray(w, np.float64) + 1j * eta
         return -self.periodized_Green_function(z, k, spin_down).imag
 
+    def dos(self, z):
+        """Density of states at complex frequency z on the wavevector grid
+        (lattice_model_instance::dos with use_grid, src_qcm/average.cpp:
+        294-347): [D_up, D_down], D = -(1/pi) Im Tr mean_K Gcpt(K, z) / L for
+        the one band of these models; z may be an array (then (nz, 2))."""
+        if GRID["k"] is None:
+            raise ValueError("set the wavevector grid first (set_wavevector_grid)")
+        nkx, nky, nkz = GRID["k"]
+        dims = (nkx, nky if self.model.dim >= 2 else 1, nkz if self.model.dim >= 3 else 1)
+        zs = np.atleast_1d(np.asarray(z, np.complex128))
+        zz = np.ascontiguousarray(zs).view(np.float64)
+        blocks = self._spin_blocks()
+        D = np.zeros((len(zs), 2))
+        for sd, blk in blocks.items():
+            L = blk.L
+            out = np.zeros(2 * len(zs) * L * L)
+            check(lib().qcmg_lattice_kmean(blk._h, len(zs), ptr(zz), dims[0], dims[1], dims[2], 0.0,
+                                           ptr(out)))
+            g = out.view(np.complex128).reshape(len(zs), L, L)
+            d = -np.trace(g, axis1=1, axis2=2).imag / np.pi / L
+            D[:, 1 if sd else 0] = d
+        if not self.cluster.mixing & 4:  # normal mixing: the down part equals the up part
+            D[:, 1] = D[:, 0]
+        return D[0] if np.ndim(z) == 0 else D
+
     def projected_Green_function(self, w, kside, spin_down=False):
         blk = self._spin_blocks()[bool(spin_down) and bool(self.cluster.mixing & 4)]
         w = as_f64(w)

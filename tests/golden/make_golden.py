@@ -3,7 +3,8 @@ exact-diagonalization code (compiled by oracle/refbuild into oracle/_ref).
 
 Run from the repository root, in a container that has the reference tree:
     make -C oracle/refbuild && python tests/golden/make_golden.py
-(`python tests/golden/make_golden.py cf` makes the continued-fraction cases only.)
+(`python tests/golden/make_golden.py cf` makes the continued-fraction cases only,
+`... lattice` the lattice cases only.)
 Each case writes <case>.npz holding the spec it ran and every array the
 reference produced (see oracle/refbuild/ref_driver.cpp for the commands).
 """
@@ -111,6 +112,10 @@ def cf_case(tag, method="F"):
 def main():
     if not os.path.exists(DRIVER):
         sys.exit("build the reference oracle first: make -C oracle/refbuild")
+    if sys.argv[1:] == ["lattice"]:  # the lattice cases only
+        for tag, c in LATTICE_CASES.items():
+            lattice_case(tag, c)
+        return
     if sys.argv[1:] == ["cf"]:  # the (matrix) continued-fraction cases only
         for tag in CF_CASES:
             cf_case(tag)
@@ -174,6 +179,8 @@ def lattice_case(tag, c):
     lines.append(f"lat_wgrid {len(w)} " + " ".join(num(x) for x in w) + " "
                  + " ".join(num(x) for x in wt))
     lines.append("lat_sef 0 sef")
+    dos_z = [complex(x, 0.1) for x in (-3.0, -1.0, -0.2, 0.0, 0.5, 2.0)]
+    lines.append(f"lat_dos 0 dos {len(dos_z)} " + " ".join(f"{z.real!r} {z.imag!r}" for z in dos_z))
     lines.append("omega 0 omega_clus")
     if nb:
         beta = 50.0
@@ -189,6 +196,7 @@ def lattice_case(tag, c):
     out["sef_wt"] = wt
     out["gper_k"] = np.array(ks)
     out["gper_z"] = np.array(zs)
+    out["dos_z"] = np.array(dos_z)
     np.savez_compressed(os.path.join(HERE, tag + ".npz"), **out)
     print(tag, sorted(k for k in out if k != "spec"))
 

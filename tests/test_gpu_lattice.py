@@ -1,5 +1,5 @@
 """GPU parity of the lattice integrals (CPT periodized G, Potthoff
-functional on a fixed grid, CDMFT host and distance) against the
+functional on a fixed grid, density of states, CDMFT host and distance) against the
 reference's QCM layer (tests/golden/lat_*.npz)."""
 import numpy as np
 import pytest
@@ -40,6 +40,22 @@ def test_potthoff_functional_grid(pg, tag):
     lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
     om = inst.Potthoff_functional()
     assert abs(om - g["sef"]) < 1e-8, (om, float(g["sef"]))
+
+
+@pytest.mark.parametrize("tag", list(LATTICE_CASES))
+def test_density_of_states_grid(pg, tag):
+    """DoS on the 8 (x 8) wavevector grid at six frequencies w + 0.1 i
+    against the reference's QCM::dos (use_grid): both spin columns.  The
+    real-axis tolerance is the CPT one (band-Lanczos poles far from the Fermi
+    level, see the Q-matrix parity note)."""
+    from pyqcm_gb300 import lattice as lat
+    g = load_golden(tag)
+    lm = build_lattice(tag)
+    inst = lm.instance()
+    lat.set_wavevector_grid(8, 8 if lm.dim >= 2 else 1, 1)
+    D = inst.dos(g["dos_z"])
+    assert D.shape == g["dos"].shape
+    assert np.max(np.abs(D - g["dos"])) < 1e-6, (tag, np.max(np.abs(D - g["dos"])))
 
 
 def test_cdmft_host_and_distance(pg):
