@@ -303,6 +303,17 @@ int qcmg_cpt_periodized(qcmg_lattice* lat, int nz, const double* z, int nk, cons
 int qcmg_lattice_kmean(qcmg_lattice* lat, int nz, const double* z, int nkx, int nky, int nkz,
                        double off, double* out);
 
+/* K moments of the CPT Green function on the same grid: for nmom (1..16)
+ * translations R_m (nmom x 3, in the basis of qcmg_lattice_create's R),
+ *   out[w][m] = mean_K exp(2 pi i K.R_m) (G(z_w)^-1 - V(K))^-1,
+ * nz x nmom blocks of L x L complex, row-major.  Every lattice average is a
+ * real linear form in these blocks: the K sum of average_integrand_k
+ * (src_qcm/average.cpp:157-190), sum_e v_e Gcpt(c_e, r_e) phase_n(e)(K),
+ * regrouped by translation, for lattice_model_instance::averages on the
+ * frequency and wavevector grids (src_qcm/average.cpp:24-105). */
+int qcmg_lattice_kmoments(qcmg_lattice* lat, int nz, const double* z, int nkx, int nky, int nkz,
+                          double off, int nmom, const double* R, double* out);
+
 /* Projected (k-averaged) CPT Green function on the midpoint grid of side
  * kside in dimk dimensions, at imaginary frequencies i w: pgf is nw blocks of
  * L x L complex, row-major.  Replaces lattice_model_instance::

@@ -33,6 +33,7 @@
 //   lat_wgrid N w_1..w_N p_1..p_N             -> discrete frequency grid
 //   lat_sef LABEL TAG                         -> QCM::Potthoff_functional
 //   lat_dos LABEL TAG NZ (re im)x NZ          -> QCM::dos on the wavevector grid
+//   lat_ave LABEL TAG OP...                   -> QCM::averages of the named operators
 //   lat_gper LABEL TAG NZ (re im)x NZ NK (kx ky kz)x NK -> periodized_Green_function
 //   lat_tk LABEL TAG NK (kx ky kz)x NK        -> QCM::tk
 //   lat_dump LABEL TAG                        -> neighbours, inter-cluster elements, H, Hc
@@ -333,6 +334,16 @@ int main(int argc, char** argv) {
       } else if (cmd == "lat_sef") {
         int label; string tag; ss >> label >> tag;
         put_scalar(tag, QCM::Potthoff_functional(label));
+      } else if (cmd == "lat_ave") {
+        // lat_ave LABEL TAG OP... : QCM::averages of the named one-body
+        // operators on the wavevector and frequency grids, in that order
+        int label; string tag, op; ss >> label >> tag;
+        vector<string> ops;
+        while (ss >> op) ops.push_back(op);
+        auto ave = QCM::averages(ops, label);
+        vector<double> v;
+        for (auto& a : ave) v.push_back(a.second);
+        put_d(tag, v);
       } else if (cmd == "lat_dos") {
         // lat_dos LABEL TAG NZ (re im)x NZ: QCM::dos on the wavevector grid,
         // one row of 2 n_band values per frequency

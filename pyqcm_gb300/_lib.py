@@ -74,6 +74,7 @@ SIGNATURES = {
     "qcmg_cpt_periodized": (c_int, [vp, c_int, vp, c_int, vp, vp]),
     "qcmg_cdmft_projected": (c_int, [vp, c_int, vp, c_int, c_int, vp]),
     "qcmg_lattice_kmean": (c_int, [vp, c_int, vp, c_int, c_int, c_int, c_double, vp]),
+    "qcmg_lattice_kmoments": (c_int, [vp, c_int, vp, c_int, c_int, c_int, c_double, c_int, vp, vp]),
     "qcmg_mlp_create": (c_int, [c_int, vp, ctypes.POINTER(vp)]),
     "qcmg_mlp_destroy": (c_int, [vp]),
     "qcmg_mlp_num_params": (c_int, [vp, size_p]),

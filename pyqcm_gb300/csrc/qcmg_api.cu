@@ -712,6 +712,19 @@ int qcmg_lattice_kmean(qcmg_lattice* h, int nz, const double* z, int nkx, int nk
   });
 }
 
+int qcmg_lattice_kmoments(qcmg_lattice* h, int nz, const double* z, int nkx, int nky, int nkz,
+                          double off, int nmom, const double* R, double* out) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(h && z && out && R, "NULL argument");
+    QCMG_CHECK_ARG(nz > 0 && nkx > 0 && nky > 0 && nkz > 0, "invalid sizes");
+    QCMG_CHECK_ARG(nmom >= 1 && nmom <= 16, "nmom must be 1..16");
+    std::lock_guard<std::mutex> lock(h->mu);
+    QCMG_CHECK_ARG(h->lat.M >= 0, "the Green function was not set");
+    QCMG_CUDA(cudaSetDevice(h->lat.device));
+    h->lat.kmoments(nz, z, nkx, nky, nkz, off, nmom, R, out, h->lat.stream);
+  });
+}
+
 int qcmg_cdmft_projected(qcmg_lattice* h, int nw, const double* w, int kside, int dimk,
                          double* pgf) {
   return guarded([&] {

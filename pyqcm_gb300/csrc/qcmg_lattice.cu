@@ -499,19 +499,40 @@ void Lattice::cpt(int nz, const double* z, int nk, const double* K, double* g, c
   QCMG_CUDA(cudaStreamSynchronize(s));
 }
 
-// sum over the midpoint grid, per frequency: out[w] = mean_K M^-1
-__global__ void k_mean_inverse(const double2* __restrict__ inv, int nw, int nk, int LL,
-                               double2* __restrict__ out) {
+// K means of the per-point inverses, per frequency and moment:
+//   out[(w nmom + m) LL + e] = (1/nk) sum_K ph[m nk + K] inv[w][K][e]
+// (ph null: one moment with phase 1).  One thread per (w, e), reading inv
+// once (consecutive threads, consecutive e) and keeping all the moments'
+// sums in registers.
+constexpr int kMaxMoments = 16;
+
+__global__ void k_mean_moments(const double2* __restrict__ inv, int nw, int nk, int LL, int nmom,
+                               const double2* __restrict__ ph, double2* __restrict__ out) {
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nw * LL;
        idx += gridDim.x * blockDim.x) {
-    int w = idx / LL, e = idx % LL;
-    double sr = 0.0, si = 0.0;
+    const int w = idx / LL, e = idx % LL;
+    double sr[kMaxMoments], si[kMaxMoments];
+#pragma unroll
+    for (int m = 0; m < kMaxMoments; ++m) sr[m] = si[m] = 0.0;
     for (int k = 0; k < nk; ++k) {
-      double2 v = inv[((size_t)w * nk + k) * LL + e];
-      sr += v.x;
-      si += v.y;
+      const double2 v = inv[((size_t)w * nk + k) * LL + e];
+      if (!ph) {
+        sr[0] += v.x;
+        si[0] += v.y;
+        continue;
+      }
+#pragma unroll
+      for (int m = 0; m < kMaxMoments; ++m) {
+        if (m < nmom) {
+          const double2 p = ph[(size_t)m * nk + k];
+          sr[m] += v.x * p.x - v.y * p.y;
+          si[m] += v.x * p.y + v.y * p.x;
+        }
+      }
     }
-    out[idx] = make_double2(sr / nk, si / nk);
+#pragma unroll
+    for (int m = 0; m < kMaxMoments; ++m)
+      if (m < nmom) out[((size_t)w * nmom + m) * LL + e] = make_double2(sr[m] / nk, si[m] / nk);
   }
 }
 
@@ -528,16 +549,38 @@ void Lattice::projected(int nw, const double* w, int kside, int dimk, double* pg
 
 void Lattice::kmean(int nz, const double* z, int gx, int gy, int gz, double off, double* out_host,
                     cudaStream_t s) {
+  kmoments(nz, z, gx, gy, gz, off, 0, nullptr, out_host, s);
+}
+
+void Lattice::kmoments(int nz, const double* z, int gx, int gy, int gz, double off, int nmom,
+                       const double* Rm, double* out_host, cudaStream_t s) {
+  QCMG_CHECK_ARG(nmom >= 0 && nmom <= kMaxMoments, "at most 16 translations per call");
   const int nk = gx * gy * gz, LL = L * L;
   const int T = point_threads(L);
   const size_t smem = (size_t)2 * L * L * T * 8;
   QCMG_CUDA(cudaFuncSetAttribute(k_points<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  // phase of each translation at each grid point, K as point_K lays it out
+  DevBuf<double> ph;
+  if (nmom > 0) {
+    std::vector<double> h((size_t)2 * nmom * nk);
+    for (int m = 0; m < nmom; ++m)
+      for (int ik = 0; ik < nk; ++ik) {
+        const int i = ik % gx, j = (ik / gx) % gy, l = ik / (gx * gy);
+        const double K0 = (i + off) / gx, K1 = gy > 1 ? (j + off) / gy : 0.0,
+                     K2 = gz > 1 ? (l + off) / gz : 0.0;
+        const double a = 2.0 * M_PI * (K0 * Rm[3 * m] + K1 * Rm[3 * m + 1] + K2 * Rm[3 * m + 2]);
+        h[2 * ((size_t)m * nk + ik)] = std::cos(a);
+        h[2 * ((size_t)m * nk + ik) + 1] = std::sin(a);
+      }
+    ph.upload(h.data(), h.size(), s);
+  }
+  const int nm = nmom > 0 ? nmom : 1;
   // frequencies in chunks whose per-point inverses fit in ~512 MB
   const size_t per_z = (size_t)nk * LL * 16;
   const int chunk = (int)std::max<size_t>(1, std::min<size_t>(nz, ((size_t)512 << 20) / per_z));
   DevBuf<double> inv, out;
   inv.alloc((size_t)2 * chunk * nk * LL);
-  out.alloc((size_t)2 * chunk * LL);
+  out.alloc((size_t)2 * chunk * nm * LL);
   for (int z0 = 0; z0 < nz; z0 += chunk) {
     const int nc = std::min(chunk, nz - z0);
     prepare(nc, z + 2 * (size_t)z0, s);
@@ -552,11 +595,12 @@ void Lattice::kmean(int nz, const double* z, int gx, int gy, int gz, double off,
     const size_t npts = (size_t)nc * nk;
     unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
     k_points<2><<<gr, T, smem, s>>>(A);
-    k_mean_inverse<<<(nc * LL + 255) / 256, 256, 0, s>>>((const double2*)inv.p, nc, nk, LL,
-                                                         (double2*)out.p);
+    k_mean_moments<<<(nc * LL + 127) / 128, 128, 0, s>>>(
+        (const double2*)inv.p, nc, nk, LL, nm, nmom > 0 ? (const double2*)ph.p : nullptr,
+        (double2*)out.p);
     QCMG_CUDA(cudaGetLastError());
-    QCMG_CUDA(cudaMemcpyAsync(out_host + (size_t)2 * z0 * LL, out.p, (size_t)2 * nc * LL * 8,
-                              cudaMemcpyDeviceToHost, s));
+    QCMG_CUDA(cudaMemcpyAsync(out_host + (size_t)2 * z0 * nm * LL, out.p,
+                              (size_t)2 * nc * nm * LL * 8, cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
   }
 }

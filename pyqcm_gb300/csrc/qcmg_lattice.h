@@ -45,6 +45,12 @@ struct Lattice {
   // out: nz x L x L complex, row-major
   void kmean(int nz, const double* z, int gx, int gy, int gz, double off, double* out,
              cudaStream_t s);
+  // the same mean with the phases of nmom (<= 16) translations R (nmom x 3,
+  // the basis of the lattice's own R):
+  //   out[w][m] = mean_K exp(2 pi i K.R_m) (G(z_w)^-1 - V(K))^-1
+  // nmom = 0: the plain mean (one L x L block per frequency)
+  void kmoments(int nz, const double* z, int gx, int gy, int gz, double off, int nmom,
+                const double* R, double* out, cudaStream_t s);
 };
 
 }  // namespace qcmg

@@ -359,6 +359,73 @@ class LatticeInstance:
             D[:, 1] = D[:, 0]
         return D[0] if np.ndim(z) == 0 else D
 
+    def averages(self, ops=None):
+        """Lattice averages of one-body operators on the frequency and wavevector
+        grids (lattice_model_instance::averages with grid_freqs,
+        src_qcm/average.cpp:24-105; integrand average_integrand_k, 157-190):
+
+            <O> = norm sum_w wt_w mean_K Re sum_e v_e [Gcpt(K, i w) - G_pole]_(c_e, r_e) phase_n(e)(K)
+
+        with G_pole = 1/(i w - 2) on the diagonal, the spin-up elements counted
+        twice when both spins share one block, and norm = 1/n_sites (mu:
+        -1/n_sites, lattice_model.cpp:383-385).  The device returns, per
+        frequency, the K means of Gcpt times each translation's phase; each
+        operator is a linear form in those blocks.  ops: names (interactions
+        are skipped, as in the reference); default every one-body operator.
+        Returns {name: value}."""
+        if GRID["w"] is None or GRID["k"] is None:
+            raise ValueError("set the k grid and the discrete frequency grid first")
+        names = [n for n, op in self.model.ops.items() if op.kind == "one-body"] if ops is None \
+            else [n for n in ops if self.model.ops[n].kind == "one-body"]
+        blocks = self._spin_blocks()
+        up_down = bool(self.cluster.mixing & 4)
+        L, no = self.model.cluster.n_sites, self.model.cluster.n_orb
+        nkx, nky, nkz = GRID["k"]
+        dims = (nkx, nky if self.model.dim >= 2 else 1, nkz if self.model.dim >= 3 else 1)
+        w, wt = GRID["w"], GRID["wt"]
+        zs = np.ascontiguousarray(1j * w)
+        gpole = 1.0 / (zs - 2.0)
+        # the K grid as the device lays it out, for the mean phase of the G_pole term
+        ax = [(np.arange(g) / g) if g > 1 else np.zeros(1) for g in dims]
+        Kg = np.stack(np.meshgrid(*ax, indexing="ij"), -1).reshape(-1, 3)
+        I = dict.fromkeys(names, 0.0)
+        for sd, blk in blocks.items():
+            off = no if sd else 0
+            inb = lambda a, b: off <= a < off + L and off <= b < off + L
+            elems, Rs = {}, [(0, 0, 0)]
+            for name in names:
+                op, lst = self.model.ops[name], []
+                for r, c, v in op.intra:  # the cluster's (r, c) and its conjugate (c, r)
+                    for a, b, x in [(r, c, v)] + ([(c, r, np.conj(v))] if r != c else []):
+                        if inb(a, b):
+                            lst.append((a - off, b - off, 0, x))
+                for r, c, n, v in op.inter:
+                    if inb(r, c):
+                        if n not in Rs:
+                            Rs.append(n)
+                        lst.append((r - off, c - off, Rs.index(n), v))
+                elems[name] = lst
+            R = np.array(Rs, np.float64)
+            mom = np.zeros((len(zs), len(Rs), L, L), np.complex128)
+            for m0 in range(0, len(Rs), 16):
+                Rc = np.ascontiguousarray(R[m0:m0 + 16])
+                out = np.zeros(2 * len(zs) * len(Rc) * L * L)
+                check(lib().qcmg_lattice_kmoments(blk._h, len(zs), ptr(zs.view(np.float64)),
+                                                  dims[0], dims[1], dims[2], 0.0, len(Rc), ptr(Rc),
+                                                  ptr(out)))
+                mom[:, m0:m0 + len(Rc)] = out.view(np.complex128).reshape(len(zs), len(Rc), L, L)
+            phm = np.exp(2j * np.pi * (Kg @ R.T)).mean(axis=0)
+            for name, lst in elems.items():
+                z = np.zeros(len(zs), np.complex128)
+                for r, c, m, v in lst:
+                    z += v * mom[:, m, c, r]
+                    if r == c:
+                        z -= v * gpole * phm[m]
+                I[name] += float(np.sum(wt * z.real))
+        norm = 1.0 / len(self.model.sites)
+        return {n: (2.0 if not up_down else 1.0) * I[n] * (-norm if n == "mu" else norm)
+                for n in names}
+
     def projected_Green_function(self, w, kside, spin_down=False):
         blk = self._spin_blocks()[bool(spin_down) and bool(self.cluster.mixing & 4)]
         w = as_f64(w)

@@ -181,6 +181,9 @@ def lattice_case(tag, c):
     lines.append("lat_sef 0 sef")
     dos_z = [complex(x, 0.1) for x in (-3.0, -1.0, -0.2, 0.0, 0.5, 2.0)]
     lines.append(f"lat_dos 0 dos {len(dos_z)} " + " ".join(f"{z.real!r} {z.imag!r}" for z in dos_z))
+    ave_ops = [op[1] for op in c["ops"] if op[0] in ("hop", "dw")]
+    ave_ops = list(dict.fromkeys(ave_ops)) + ["mu"]
+    lines.append("lat_ave 0 ave " + " ".join(ave_ops))
     lines.append("omega 0 omega_clus")
     if nb:
         beta = 50.0
@@ -197,6 +200,7 @@ def lattice_case(tag, c):
     out["gper_k"] = np.array(ks)
     out["gper_z"] = np.array(zs)
     out["dos_z"] = np.array(dos_z)
+    out["ave_ops"] = np.array(ave_ops)
     np.savez_compressed(os.path.join(HERE, tag + ".npz"), **out)
     print(tag, sorted(k for k in out if k != "spec"))
 

@@ -69,3 +69,21 @@ def test_cdmft_host_and_distance(pg):
     d1 = inst.CDMFT_distance({"eb1_1": -1.2, "eb2_1": 0.8, "tb1_1": 0.45})
     assert abs(d0 - g["dist0"]) < 1e-10 * max(1.0, abs(float(g["dist0"])))
     assert abs(d1 - g["dist1"]) < 1e-10 * max(1.0, abs(float(g["dist1"])))
+
+
+@pytest.mark.parametrize("tag", list(LATTICE_CASES))
+def test_lattice_averages_grid(pg, tag):
+    """Averages of the one-body operators (t, the density wave, mu) on the
+    Potthoff-functional grids against the reference's QCM::averages (grid
+    frequencies, wavevector grid)."""
+    from pyqcm_gb300 import lattice as lat
+    g = load_golden(tag)
+    lm = build_lattice(tag)
+    inst = lm.instance()
+    lat.set_wavevector_grid(8, 8 if lm.dim >= 2 else 1, 1)
+    lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
+    names = [str(n) for n in g["ave_ops"]]
+    ave = inst.averages(names)
+    assert list(ave) == names
+    got = np.array([ave[n] for n in names])
+    assert np.max(np.abs(got - g["ave"])) < 1e-9, (tag, got, g["ave"])
