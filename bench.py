@@ -441,31 +441,29 @@ def cdmft_instances(n, n_bath, seed=0):
 
 
 def run_cdmft(args):
-    """CDMFT loops of the plaquette + bath model to convergence, one after the
-    other on the device: converged points per hour."""
+    """CDMFT loops of the plaquette + bath model to convergence, `--concurrency`
+    loops in flight at a time on the device: converged points per hour."""
     import numpy as np
     import torch
-    from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model
+    from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model, run_many
     torch.cuda.set_device(0)
     nb = args.bath or 8
     sector = {4: "R0:N8:S0", 8: "R0:N12:S0"}[nb]
     names = bath_names(nb)
-    rows = []
-    t_all = time.perf_counter()
+    loops = []
     for U, mu, eb, tb in cdmft_instances(args.samples, nb, seed=args.seed):
         lm = plaquette_bath_model(nb, sector)
         params = {"t": 1.0, "tp": 0.0, "U": U, "mu": mu}
         params.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
         lm.set_parameters(params)
-        c = CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64)
-        t0 = time.perf_counter()
-        ok, why = True, ""
-        try:
-            c.run()
-        except Exception as e:  # a failed instance is reported, the others still run
-            ok, why = False, f"{type(e).__name__}: {e}"[:160]
-        rows.append((ok, max(c.niter, len(c.history)), time.perf_counter() - t0, c.time_ed,
-                     c.time_fit, c.dist, why))
+        loops.append(CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64))
+    t_all = time.perf_counter()
+    res = run_many(loops, workers=args.concurrency)
+    rows = []
+    for c, (x, secs, err) in zip(loops, res):
+        why = "" if err is None else f"{type(err).__name__}: {err}"[:160]
+        rows.append((err is None, max(c.niter, len(c.history)), secs, c.time_ed, c.time_fit,
+                     c.dist, why))
     total = time.perf_counter() - t_all
     conv = [r for r in rows if r[0]]
     failures = sorted({r[6] for r in rows if not r[0]})
@@ -475,6 +473,7 @@ def run_cdmft(args):
         "converged": len(conv), "mean_iterations": float(np.mean([r[1] for r in rows])),
         "s_per_point": total / max(len(rows), 1),
         "s_per_iteration": sum(r[2] for r in rows) / max(sum(r[1] for r in rows), 1),
+        "concurrency": args.concurrency,
         "impurity_and_host_s": sum(r[3] for r in rows), "bath_fit_s": sum(r[4] for r in rows),
         "failures": failures, "iteration": "broyden",
         "dtype": "f64", "data": "synthetic",
@@ -537,6 +536,8 @@ def main():
                          "training set is the 4-bath one)")
     ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
+    ap.add_argument("--concurrency", type=int, default=8,
+                    help="CDMFT loops in flight at a time (one host thread each)")
     ap.add_argument("--warm-data", default=None, help="training set of the warm-start workload")
     ap.add_argument("--epochs", type=int, default=20000, help="training epochs of the warm-start MLP")
     args = ap.parse_args()

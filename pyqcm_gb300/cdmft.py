@@ -302,6 +302,31 @@ class CDMFT:
         return self.xs
 
 
+def run_many(loops, workers=4):
+    """Runs independent CDMFT loops concurrently, one host thread per loop in
+    flight.  Each loop owns its lattice model and, through it, its device
+    handles and CUDA streams; the library's calls release the GIL, so one
+    loop's kernels and host waits overlap the others' impurity solves, host
+    functions and bath fits.  Returns [(x, seconds, error)] in the order of
+    `loops` (x None and error the exception when a loop failed)."""
+    from concurrent.futures import ThreadPoolExecutor
+    from . import lib
+    lib()  # load the library before the threads start
+
+    def one(c):
+        t0 = time.perf_counter()
+        try:
+            x = c.run()
+            return x, time.perf_counter() - t0, None
+        except Exception as e:  # reported per loop; the others still run
+            return None, time.perf_counter() - t0, e
+
+    if workers <= 1:
+        return [one(c) for c in loops]
+    with ThreadPoolExecutor(max_workers=workers) as ex:
+        return list(ex.map(one, loops))
+
+
 def plaquette_bath_model(n_bath=8, sector="R0:N12:S0"):
     """The 2x2 plaquette with n_bath bath orbitals on the square lattice
     (bath k: energy eb{k+1}, hybridization tb{k+1} with site k % 4), with

@@ -41,3 +41,27 @@ def test_cdmft_same_solution_from_a_perturbed_start(pg):
     e1, t1 = np.sort(x1[:4]), np.sort(np.abs(x1[4:]))
     e2, t2 = np.sort(x2[:4]), np.sort(np.abs(x2[4:]))
     assert np.max(np.abs(e1 - e2)) < 1e-3 and np.max(np.abs(t1 - t2)) < 1e-3, (x1, x2)
+
+
+def test_concurrent_loops_match_sequential_runs(pg):
+    """Two loops in flight at once (run_many, one host thread each, separate
+    device handles and streams) converge to the same baths as the same loops
+    run one after the other: the engine's reductions are deterministic, so
+    the results agree to rounding."""
+    from lattice_helpers import build_lattice
+    from pyqcm_gb300.cdmft import CDMFT, run_many
+    names = ["eb1_1", "eb2_1", "eb3_1", "eb4_1", "tb1_1", "tb2_1", "tb3_1", "tb4_1"]
+
+    def loops():
+        out = []
+        for U in (4.0, 6.0):
+            lm = build_lattice("lat_cdmft2x2_b4")
+            lm.set_parameters(dict(lm.params, U=U, mu=U / 2))
+            out.append(CDMFT(lm, names, grid=(39 * np.pi / 50, 50.0), kside=8, maxiter=60))
+        return out
+
+    seq = run_many(loops(), workers=1)
+    par = run_many(loops(), workers=2)
+    for (xs, _, es), (xp, _, ep) in zip(seq, par):
+        assert es is None and ep is None, (es, ep)
+        assert np.max(np.abs(xs - xp)) < 1e-12, (xs, xp)
