@@ -442,7 +442,8 @@ def cdmft_instances(n, n_bath, seed=0):
 
 def run_cdmft(args):
     """CDMFT loops of the plaquette + bath model to convergence, `--concurrency`
-    loops in flight at a time on the device: converged points per hour."""
+    loops in flight at a time on the device (host threads, one loop each):
+    converged points per hour."""
     import numpy as np
     import torch
     from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model, run_many
@@ -459,12 +460,12 @@ def run_cdmft(args):
         loops.append(CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64))
     t_all = time.perf_counter()
     res = run_many(loops, workers=args.concurrency)
+    total = time.perf_counter() - t_all
     rows = []
     for c, (x, secs, err) in zip(loops, res):
         why = "" if err is None else f"{type(err).__name__}: {err}"[:160]
         rows.append((err is None, max(c.niter, len(c.history)), secs, c.time_ed, c.time_fit,
                      c.dist, why))
-    total = time.perf_counter() - t_all
     conv = [r for r in rows if r[0]]
     failures = sorted({r[6] for r in rows if not r[0]})
     print(json.dumps({

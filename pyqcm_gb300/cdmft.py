@@ -331,8 +331,8 @@ def plaquette_bath_model(n_bath=8, sector="R0:N12:S0"):
     """The 2x2 plaquette with n_bath bath orbitals on the square lattice
     (bath k: energy eb{k+1}, hybridization tb{k+1} with site k % 4), with
     lattice operators t (nearest neighbour), tp (diagonal), U and the built-in
-    mu: the CDMFT benchmark model (BASELINE configs' batched CDMFT case with
-    one hybridization per bath orbital)."""
+    mu: the batched-CDMFT benchmark model, with one hybridization per bath
+    orbital."""
     from .lattice import LatticeModel
     ns, no = 4, 4 + n_bath
     cm = ClusterModel(ns, n_bath)
