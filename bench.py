@@ -452,7 +452,7 @@ def run_cdmft(args):
     sector = {4: "R0:N8:S0", 8: "R0:N12:S0"}[nb]
     names = bath_names(nb)
     loops = []
-    for U, mu, eb, tb in cdmft_instances(args.samples, nb, seed=args.seed):
+    for U, mu, eb, tb in cdmft_instances(args.samples or 32, nb, seed=args.seed):
         lm = plaquette_bath_model(nb, sector)
         params = {"t": 1.0, "tp": 0.0, "U": U, "mu": mu}
         params.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
@@ -498,7 +498,7 @@ def run_warmstart(args):
     t0 = time.perf_counter()
     m, loss = ws.train(P, Y, epochs=args.epochs)
     t_train = time.perf_counter() - t0
-    Ptest = ws.sample_params(args.samples, seed=args.seed + 1000)  # held out: another seed
+    Ptest = ws.sample_params(args.samples or 3, seed=args.seed + 1000)  # held out: another seed
     res = ws.evaluate(m, Ptest, nb)
     s_plain = sum(r["s_plain"] for r in res)
     s_warm = sum(r["s_warm"] for r in res)
@@ -535,7 +535,9 @@ def main():
     ap.add_argument("--bath", type=int, default=None, choices=[4, 8],
                     help="bath orbitals (default: 8 for cdmft, 4 for warmstart, whose "
                          "training set is the 4-bath one)")
-    ap.add_argument("--samples", type=int, default=3, help="instances of the CDMFT workload")
+    ap.add_argument("--samples", type=int, default=None,
+                    help="instances of the CDMFT workload (default 32) or held-out points of "
+                         "the warm-start workload (default 3)")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
     ap.add_argument("--concurrency", type=int, default=8,
                     help="CDMFT loops in flight at a time (one host thread each)")
