@@ -344,6 +344,11 @@ int main(int argc, char** argv) {
         vector<double> v;
         for (auto& a : ave) v.push_back(a.second);
         put_d(tag, v);
+      } else if (cmd == "lat_pe") {
+        // lat_pe LABEL TAG : QCM::potential_energy on the wavevector and
+        // frequency grids
+        int label; string tag; ss >> label >> tag;
+        put_scalar(tag, QCM::potential_energy(label));
       } else if (cmd == "lat_dos") {
         // lat_dos LABEL TAG NZ (re im)x NZ: QCM::dos on the wavevector grid,
         // one row of 2 n_band values per frequency

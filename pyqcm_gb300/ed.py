@@ -741,6 +741,24 @@ class ModelInstance:
             S = S + self.hybridization_function_many(zs, spin_down)
         return zs[:, None, None] * np.eye(len(tc))[None] - S
 
+    def tr_sigma_inf(self):
+        """Trace of the self-energy's infinite-frequency limit
+        (model_instance::tr_sigma_inf, src_ed/model_instance.hpp:1279-1311):
+        Re Tr Sigma(i/x) at x = 1e-5, 2e-5 and 3e-5, summed over the spin
+        blocks (twice the one block when both spins share it), and the
+        quadratic through those three points evaluated at x = 0 (the
+        reference's Neville scheme; the same polynomial in Lagrange form)."""
+        x = np.array([1e-5, 2e-5, 3e-5])
+        zs = 1j / x
+        S = np.zeros(len(x))
+        for sd in ((False, True) if self.mixing & 4 else (False,)):
+            S += np.trace(self.self_energy_many(zs, sd), axis1=1, axis2=2).real
+        if not self.mixing & 4:
+            S *= 2.0
+        lag = [np.prod([-x[j] / (x[i] - x[j]) for j in range(len(x)) if j != i])
+               for i in range(len(x))]
+        return float(np.dot(lag, S))
+
     def SEF_bath(self):
         sef = 0.0
         for sd in ((False, True) if self.mixing & 4 else (False,)):

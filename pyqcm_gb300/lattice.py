@@ -8,6 +8,7 @@ of pyqcm's lattice interface that feeds the k x omega integrals:
   LatticeInstance   ~ lattice_model_instance (src_qcm/lattice_model_instance.cpp):
                       Potthoff_functional on a fixed (k, omega) grid,
                       periodized_Green_function / spectral_function (CPT),
+                      dos, averages and potential_energy on the fixed grids,
                       CDMFT_host, CDMFT_distance
 Wavevectors passed by the user are in units of 2 pi / a of the physical
 lattice (the reference's physdual basis); internally K = S k with S the
@@ -425,6 +426,39 @@ class LatticeInstance:
         norm = 1.0 / len(self.model.sites)
         return {n: (2.0 if not up_down else 1.0) * I[n] * (-norm if n == "mu" else norm)
                 for n in names}
+
+    def potential_energy(self):
+        """Potential energy per site on the frequency and wavevector grids
+        (lattice_model_instance::potential_energy with grid_freqs,
+        src_qcm/average.cpp:530-584; integrand potential_energy_integrand_k,
+        669-686):
+
+            E_pot = (1/2L) sum_w wt_w Re[ s Tr(Sigma(i w) mean_K Gcpt(K, i w)) - tr_sigma_inf/(i w - 2) ]
+
+        with s = 2 when both spins share one block (else the blocks are
+        summed).  Sigma does not depend on K, so the K sum is the device's K
+        mean of Gcpt, the same one as the density of states."""
+        if GRID["w"] is None or GRID["k"] is None:
+            raise ValueError("set the k grid and the discrete frequency grid first")
+        blocks = self._spin_blocks()
+        up_down = bool(self.cluster.mixing & 4)
+        nkx, nky, nkz = GRID["k"]
+        dims = (nkx, nky if self.model.dim >= 2 else 1, nkz if self.model.dim >= 3 else 1)
+        w, wt = GRID["w"], GRID["wt"]
+        zs = np.ascontiguousarray(1j * w)
+        tr = np.zeros(len(zs), np.complex128)
+        for sd, blk in blocks.items():
+            L = blk.L
+            out = np.zeros(2 * len(zs) * L * L)
+            check(lib().qcmg_lattice_kmean(blk._h, len(zs), ptr(zs.view(np.float64)), dims[0],
+                                           dims[1], dims[2], 0.0, ptr(out)))
+            g = out.view(np.complex128).reshape(len(zs), L, L)
+            S = self.cluster.self_energy_many(zs, sd)
+            tr += np.einsum("wij,wji->w", S, g)
+        if not up_down:
+            tr *= 2.0
+        e = tr - self.cluster.tr_sigma_inf() / (zs - 2.0)
+        return 0.5 * float(np.sum(wt * e.real)) / len(self.model.sites)
 
     def projected_Green_function(self, w, kside, spin_down=False):
         blk = self._spin_blocks()[bool(spin_down) and bool(self.cluster.mixing & 4)]

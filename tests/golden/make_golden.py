@@ -184,6 +184,7 @@ def lattice_case(tag, c):
     ave_ops = [op[1] for op in c["ops"] if op[0] in ("hop", "dw")]
     ave_ops = list(dict.fromkeys(ave_ops)) + ["mu"]
     lines.append("lat_ave 0 ave " + " ".join(ave_ops))
+    lines.append("lat_pe 0 epot")
     lines.append("omega 0 omega_clus")
     if nb:
         beta = 50.0

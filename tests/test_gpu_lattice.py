@@ -87,3 +87,18 @@ def test_lattice_averages_grid(pg, tag):
     assert list(ave) == names
     got = np.array([ave[n] for n in names])
     assert np.max(np.abs(got - g["ave"])) < 1e-9, (tag, got, g["ave"])
+
+
+@pytest.mark.parametrize("tag", list(LATTICE_CASES))
+def test_potential_energy_grid(pg, tag):
+    """Potential energy per site on the Potthoff-functional grids against the
+    reference's QCM::potential_energy (grid frequencies, wavevector grid),
+    including its extrapolated Tr Sigma(infinity)."""
+    from pyqcm_gb300 import lattice as lat
+    g = load_golden(tag)
+    lm = build_lattice(tag)
+    inst = lm.instance()
+    lat.set_wavevector_grid(8, 8 if lm.dim >= 2 else 1, 1)
+    lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
+    e = inst.potential_energy()
+    assert abs(e - g["epot"]) < 1e-8, (tag, e, float(g["epot"]))
