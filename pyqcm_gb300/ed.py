@@ -549,6 +549,59 @@ class ModelInstance:
                 st.gf_down = solve(st, True)
         self.gf_solved = True
 
+    def write_qmatrix(self, path):
+        """Saves the solved instance's Lehmann data, so that the lattice stage can
+        run from the file without the impurity solve.  Per kept state and spin
+        block, the Q-matrix datasets of the reference's Q_matrix::write_hdf5
+        (src_ed/Q_matrix.hpp:322-332: L, M, e, v), with the state's sector,
+        energy and weight, and the instance's parameter values, mixing and
+        energies.  The container is a NumPy .npz archive, since no HDF5 library
+        is part of this package.  Needs GF_method 'L'."""
+        if self.gf_method != "L":
+            raise ValueError("Q-matrix files need GF_method 'L'")
+        self.Green_function_solve()
+        names = sorted(self.values)
+        d = {"value_names": np.array(names), "values": np.array([self.values[n] for n in names]),
+             "mixing": self.mixing, "GS_energy": self.GS_energy, "E0": self.E0,
+             "n_states": len(self.states)}
+        for i, st in enumerate(self.states):
+            d[f"s{i}_sector"] = np.array(st.sec.name())
+            d[f"s{i}_energy"] = st.energy
+            d[f"s{i}_weight"] = st.weight
+            for tag, blk in (("up", st.gf), ("down", st.gf_down)):
+                if blk is None:
+                    continue
+                e, v = blk
+                d[f"s{i}_{tag}_L"], d[f"s{i}_{tag}_M"] = v.shape[0], len(e)
+                d[f"s{i}_{tag}_e"], d[f"s{i}_{tag}_v"] = e, v
+        np.savez_compressed(path, **d)
+
+    def read_qmatrix(self, path):
+        """Restores what write_qmatrix saved: the instance is then solved (ground
+        state and Green function) with no device work.  The file's parameter
+        values must be this instance's."""
+        with np.load(path) as f:
+            vals = dict(zip([str(n) for n in f["value_names"]], f["values"].tolist()))
+            if vals.keys() != self.values.keys() or any(
+                    abs(vals[n] - self.values[n]) > 1e-14 * max(1.0, abs(vals[n])) for n in vals):
+                raise ValueError("the Q-matrix file was written for other parameter values")
+            states = []
+            for i in range(int(f["n_states"])):
+                st = State(Sector(str(f[f"s{i}_sector"])), float(f[f"s{i}_energy"]), None)
+                st.weight = float(f[f"s{i}_weight"])
+                for tag in ("up", "down"):
+                    if f"s{i}_{tag}_e" in f.files:
+                        e, v = f[f"s{i}_{tag}_e"], f[f"s{i}_{tag}_v"]
+                        if v.shape != (int(f[f"s{i}_{tag}_L"]), int(f[f"s{i}_{tag}_M"])):
+                            raise ValueError("inconsistent Q-matrix block in the file")
+                        setattr(st, "gf" if tag == "up" else "gf_down", (e, v))
+                states.append(st)
+            self.states = states
+            self.mixing = int(f["mixing"])
+            self.GS_energy, self.E0 = float(f["GS_energy"]), float(f["E0"])
+        self.gf_method = "L"
+        self.gs_solved = self.gf_solved = True
+
     def _cf_state(self, st, spin_down):
         """Continued fractions of one state, as model_instance<double>::build_cf
         (model_instance.cpp:35-100): for every orbital pair o2 <= o1, the

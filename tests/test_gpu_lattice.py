@@ -102,3 +102,23 @@ def test_potential_energy_grid(pg, tag):
     lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
     e = inst.potential_energy()
     assert abs(e - g["epot"]) < 1e-8, (tag, e, float(g["epot"]))
+
+
+def test_lattice_stage_from_a_qmatrix_file(pg, tmp_path):
+    """The impurity stage written to a Q-matrix file and read back by a fresh
+    instance gives the same Potthoff functional and CPT Green function, with
+    no impurity solve in the second instance."""
+    from pyqcm_gb300 import lattice as lat
+    g = load_golden("lat_vca2x2_af")
+    lat.set_wavevector_grid(8, 8, 1)
+    lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
+    a = build_lattice("lat_vca2x2_af").instance()
+    om_a = a.Potthoff_functional()
+    G_a = a.periodized_Green_function(g["gper_z"], g["gper_k"])
+    path = tmp_path / "vca.npz"
+    a.cluster.write_qmatrix(path)
+    b = build_lattice("lat_vca2x2_af").instance()
+    b.cluster.read_qmatrix(path)
+    assert not b.cluster._H  # no sector Hamiltonian was built
+    assert b.Potthoff_functional() == om_a
+    assert np.array_equal(b.periodized_Green_function(g["gper_z"], g["gper_k"]), G_a)
