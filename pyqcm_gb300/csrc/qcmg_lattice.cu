@@ -18,7 +18,10 @@
 // with its matrix in shared memory (interleaved across threads, no bank
 // conflicts).
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
+#include <map>
+#include <mutex>
 #include <vector>
 
 #include "qcmg_internal.h"
@@ -354,6 +357,57 @@ static int point_threads(int L) {
   return T;
 }
 
+// Block size of the SEF point kernel, tuned once per matrix dimension L and
+// process: each candidate (multiples of 32 whose matrices fit the shared
+// memory budget, at most four, largest first) runs the same launch on the
+// caller's first frequencies (as many as one launch of that shape takes),
+// timed with CUDA events after one untimed run; the least time per
+// frequency is kept.  QCMG_POINT_THREADS overrides the choice;
+// QCMG_VERBOSE reports it on stderr.
+static std::mutex g_tune_mu;
+static std::map<int, int> g_tuned_sef;
+
+template <class Launch>
+static int tuned_sef_threads(int L, Launch&& launch, cudaStream_t s) {
+  if (std::getenv("QCMG_POINT_THREADS")) return point_threads(L);
+  {
+    std::lock_guard<std::mutex> lock(g_tune_mu);
+    auto it = g_tuned_sef.find(L);
+    if (it != g_tuned_sef.end()) return it->second;
+  }
+  const int tmax = point_threads(L);
+  std::vector<int> cand;
+  for (int T = tmax; T >= 32 && cand.size() < 4; T -= 32) cand.push_back(T);
+  cudaEvent_t e0, e1;
+  QCMG_CUDA(cudaEventCreate(&e0));
+  QCMG_CUDA(cudaEventCreate(&e1));
+  int best = tmax;
+  float best_ms = 0.0f;
+  for (int T : cand) {
+    launch(T);  // untimed: first-launch costs
+    QCMG_CUDA(cudaEventRecord(e0, s));
+    const int nf = launch(T);  // frequencies this launch covered
+    QCMG_CUDA(cudaEventRecord(e1, s));
+    QCMG_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.0f;
+    QCMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    ms /= (float)nf;
+    if (T == cand.front() || ms < best_ms) {
+      best_ms = ms;
+      best = T;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (std::getenv("QCMG_VERBOSE"))
+    std::fprintf(stderr,
+                 "qcmg: SEF point kernel, L = %d: %d threads per block (%.3f ms per frequency)\n",
+                 L, best, best_ms);
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  g_tuned_sef[L] = best;
+  return best;
+}
+
 void Lattice::prepare(int nw, const double* z, cudaStream_t s) {
   QCMG_CHECK_ARG(L > 0 && L <= 32, "lattice Green function dimension must be 1..32");
   QCMG_CHECK_ARG(M >= 0, "Q-matrix not set");
@@ -441,20 +495,19 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   // frequencies are processed one by one so the per-frequency weight is
   // applied exactly; each launch covers the whole K grid
   prepare(nw, z.data(), s);
-  const int T = point_threads(L);
-  const size_t smem = (size_t)2 * L * L * T * 8;
-  QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  DevBuf<double> part;
   const double2* phases = (const double2*)phase_tables(nkx, nky, nkz, 0.0, s);
   // Several frequencies per launch (enough blocks for many waves on every
   // SM), with each block's partial sum tied to one frequency, so the
   // weights are still applied to whole per-frequency sums.
-  const unsigned bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
-  const int fpl = std::max(1, std::min(nw, (int)((152u * 16u + bpf - 1) / bpf)));
-  part.alloc((size_t)bpf * fpl);
-  std::vector<double> hp((size_t)bpf * fpl);
-  for (int i0 = 0; i0 < nw; i0 += fpl) {
-    const int nf = std::min(fpl, nw - i0);
+  auto shape = [&](int T, unsigned& bpf, int& fpl) {
+    bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
+    fpl = std::max(1, std::min(nw, (int)((152u * 16u + bpf - 1) / bpf)));
+  };
+  DevBuf<double> part;
+  auto launch = [&](int T, int i0, int nf, unsigned bpf) {
+    const size_t smem = (size_t)2 * L * L * T * 8;
+    QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   (int)smem));
     PointArgs A = point_args(*this, nf);
     A.base = (const double2*)base.p + (size_t)i0 * L * L;
     A.nk = nk;
@@ -468,6 +521,27 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     A.tab = phases;
     k_points<0><<<bpf * nf, T, smem, s>>>(A);
     QCMG_CUDA(cudaGetLastError());
+  };
+  const int T = tuned_sef_threads(
+      L,
+      [&](int Tc) {
+        unsigned b;
+        int f;
+        shape(Tc, b, f);
+        if (part.n < (size_t)b * f) part.alloc((size_t)b * f);
+        const int nf = std::min(f, nw);
+        launch(Tc, 0, nf, b);
+        return nf;
+      },
+      s);
+  unsigned bpf;
+  int fpl;
+  shape(T, bpf, fpl);
+  if (part.n < (size_t)bpf * fpl) part.alloc((size_t)bpf * fpl);
+  std::vector<double> hp((size_t)bpf * fpl);
+  for (int i0 = 0; i0 < nw; i0 += fpl) {
+    const int nf = std::min(fpl, nw - i0);
+    launch(T, i0, nf, bpf);
     QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
     for (int f = 0; f < nf; ++f) {
