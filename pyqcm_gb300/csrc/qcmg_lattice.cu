@@ -575,21 +575,28 @@ void Lattice::cpt(int nz, const double* z, int nk, const double* K, double* g, c
 
 // K means of the per-point inverses, per frequency and moment:
 //   out[(w nmom + m) LL + e] = (1/nk) sum_K ph[m nk + K] inv[w][K][e]
-// (ph null: one moment with phase 1).  One thread per (w, e), reading inv
-// once (consecutive threads, consecutive e) and keeping all the moments'
-// sums in registers.
+// (ph null: one moment with phase 1).  One block per (frequency, 32
+// consecutive elements e): the lanes take consecutive e (coalesced loads of
+// each point's block), the warps interleave over K, and every moment's sums
+// stay in registers until a fixed-order reduction over the warps in shared
+// memory.
 constexpr int kMaxMoments = 16;
+constexpr int kMomWarps = 8;
 
-__global__ void k_mean_moments(const double2* __restrict__ inv, int nw, int nk, int LL, int nmom,
-                               const double2* __restrict__ ph, double2* __restrict__ out) {
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nw * LL;
-       idx += gridDim.x * blockDim.x) {
-    const int w = idx / LL, e = idx % LL;
-    double sr[kMaxMoments], si[kMaxMoments];
+__global__ void __launch_bounds__(32 * kMomWarps)
+    k_mean_moments(const double2* __restrict__ inv, int nw, int nk, int LL, int nmom,
+                   const double2* __restrict__ ph, double2* __restrict__ out) {
+  __shared__ double red[2][kMomWarps][32];
+  const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+  const int w = blockIdx.x, e = blockIdx.y * 32 + lane;
+  const int nm = ph ? nmom : 1;
+  double sr[kMaxMoments], si[kMaxMoments];
 #pragma unroll
-    for (int m = 0; m < kMaxMoments; ++m) sr[m] = si[m] = 0.0;
-    for (int k = 0; k < nk; ++k) {
-      const double2 v = inv[((size_t)w * nk + k) * LL + e];
+  for (int m = 0; m < kMaxMoments; ++m) sr[m] = si[m] = 0.0;
+  if (e < LL) {
+    const double2* col = inv + (size_t)w * nk * LL + e;
+    for (int k = wp; k < nk; k += kMomWarps) {
+      const double2 v = col[(size_t)k * LL];
       if (!ph) {
         sr[0] += v.x;
         si[0] += v.y;
@@ -597,16 +604,30 @@ __global__ void k_mean_moments(const double2* __restrict__ inv, int nw, int nk, 
       }
 #pragma unroll
       for (int m = 0; m < kMaxMoments; ++m) {
-        if (m < nmom) {
+        if (m < nm) {
           const double2 p = ph[(size_t)m * nk + k];
           sr[m] += v.x * p.x - v.y * p.y;
           si[m] += v.x * p.y + v.y * p.x;
         }
       }
     }
+  }
 #pragma unroll
-    for (int m = 0; m < kMaxMoments; ++m)
-      if (m < nmom) out[((size_t)w * nmom + m) * LL + e] = make_double2(sr[m] / nk, si[m] / nk);
+  for (int m = 0; m < kMaxMoments; ++m) {
+    if (m < nm) {  // the same for the whole block
+      red[0][wp][lane] = sr[m];
+      red[1][wp][lane] = si[m];
+      __syncthreads();
+      if (wp == 0 && e < LL) {
+        double a = 0.0, b = 0.0;
+        for (int q = 0; q < kMomWarps; ++q) {
+          a += red[0][q][lane];
+          b += red[1][q][lane];
+        }
+        out[((size_t)w * nm + m) * LL + e] = make_double2(a / nk, b / nk);
+      }
+      __syncthreads();
+    }
   }
 }
 
@@ -669,7 +690,7 @@ void Lattice::kmoments(int nz, const double* z, int gx, int gy, int gz, double o
     const size_t npts = (size_t)nc * nk;
     unsigned gr = (unsigned)std::max<size_t>(1, std::min<size_t>((npts + T - 1) / T, 152 * 8));
     k_points<2><<<gr, T, smem, s>>>(A);
-    k_mean_moments<<<(nc * LL + 127) / 128, 128, 0, s>>>(
+    k_mean_moments<<<dim3(nc, (LL + 31) / 32), 32 * kMomWarps, 0, s>>>(
         (const double2*)inv.p, nc, nk, LL, nm, nmom > 0 ? (const double2*)ph.p : nullptr,
         (double2*)out.p);
     QCMG_CUDA(cudaGetLastError());
