@@ -256,6 +256,33 @@ def run_gpu(args):
     achieved = bytes_step / (avg_launch_ms * 1e-3) / 1e9
     peak, peak_kind = measured_peak()
 
+    # The FP64 product (k_matvec_f64, any hop values) on the same sector and
+    # vectors: the arithmetic the reference's mult_add performs, timed the
+    # same way; the fixed-point line above is the fast path of this product.
+    fp64 = None
+    if fast and not args.no_fp64:
+        yf = x.clone()
+        H.set_path(False)
+        stepf = lambda: H.matvec_device(x.data_ptr(), yf.data_ptr(), asynchronous=True,
+                                        accumulate=True)
+        for _ in range(max(args.warmup, 3)):
+            stepf()
+        nf = max(3, min(args.steps, 10))
+        f0 = torch.cuda.Event(enable_timing=True)
+        f1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        f0.record(stream)
+        for _ in range(nf):
+            stepf()
+        f1.record(stream)
+        torch.cuda.synchronize()
+        H.set_path(True)
+        ms_f = f0.elapsed_time(f1) / nf
+        gbs_f = bytes_step / (ms_f * 1e-3) / 1e9
+        fp64 = {"value": gbs_f, "unit": UNIT, "ms_per_step": ms_f, "steps": nf,
+                "frac": gbs_f / peak, "kernels": ["k_matvec_f64"], "dtype": "f64"}
+        del yf
+
     # e2e through the public host API (Hamiltonian.mult_add, the reference's
     # mult_add): pinned host x and y in, y out, every step.
     xh = torch.empty(D, dtype=torch.float64, pin_memory=True)
@@ -284,6 +311,8 @@ def run_gpu(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 16 * D,
                     "d2h_bytes_per_step": 8 * D},
             "gpu_launches": args.steps * len(kernels)}
+    if fp64:
+        line["fp64_product"] = fp64
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
         gbs, dt = cpu_port_timing(1, threads)
@@ -525,6 +554,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="qcmg", choices=["qcmg", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the FP64 product measured beside the fixed-point one")
     ap.add_argument("--cluster", default="4x4",
                     help="NXxNY Hubbard cluster at half filling (profiling of smaller cases)")
     ap.add_argument("--electrons", type=int, default=None,

@@ -12,6 +12,9 @@
 //   halfbasis L N                             -> ED_halfbasis bin list
 //   hamiltonian MODEL SECTOR TAG              -> Hamiltonian_Factorized: half-operators, x0, H.x0
 //   lanczos MODEL SECTOR TAG                  -> LanczosEigenvalue/Eigenvector from x0
+//   hcheck MODEL SECTOR TAG                   -> one timed mult_add on x0: sum, norm^2, <x0,Hx0>,
+//                                                4096 sampled elements (large sectors)
+//   lanczos_e0 MODEL SECTOR TAG               -> LanczosEigenvalue from x0: E0, alpha, beta, time
 //   destroy MODEL SECTOR ORB SPIN PM TAG      -> c / c^dagger applied to x0 (factorized branch)
 //   gs LABEL TAG                              -> ED::ground_state_solve
 //   qmatrix LABEL SPIN TAG                    -> ED::Green_function_solve + ED::qmatrix
@@ -40,6 +43,7 @@
 //   lat_varia NAME...                         -> QCM::CDMFT_variational_set (cluster 0)
 //   lat_host LABEL TAG NW w.. wt..            -> QCM::CDMFT_host (+ get_CDMFT_host)
 //   lat_dist LABEL TAG NP p..                 -> QCM::CDMFT_distance (cluster 0)
+#include <chrono>
 #include <complex>
 #include <cstdio>
 #include <fstream>
@@ -233,6 +237,53 @@ int main(int argc, char** argv) {
           put_scalar(tag + "_E0", energy[0]);
           LanczosEigenvector(H, gs, alpha, beta, false);
           put_d(tag + "_psi", gs);
+        }
+      } else if (cmd == "hcheck" || cmd == "lanczos_e0") {
+        // Large sectors: no vector is written.  hcheck: one timed mult_add on
+        // the seeded start x0, reduced to scalars and a fixed sample of y;
+        // lanczos_e0: LanczosEigenvalue only (energy, alpha, beta, time).
+        string m, secs, tag; ss >> m >> secs >> tag;
+        create_ops(S, m);
+        auto mod = models.at(m);
+        if (!mod->is_factorized)
+          throw runtime_error("model " + m + " is not factorized: create an instance with format F first");
+        sector sec(secs);
+        auto v = values_for(S, m);
+        Hamiltonian_Factorized<double> H(mod, v, sec);
+        vector<double> x0 = seeded_start(H.dim);
+        if (cmd == "hcheck") {
+          vector<double> y(H.dim, 0.0);
+          auto t0 = chrono::steady_clock::now();
+          H.mult_add(x0, y);
+          double sec_s = chrono::duration<double>(chrono::steady_clock::now() - t0).count();
+          double s1 = 0, s2 = 0, sxy = 0;
+          for (size_t i = 0; i < H.dim; i++) { s1 += y[i]; s2 += y[i] * y[i]; sxy += x0[i] * y[i]; }
+          put_scalar(tag + "_sum", s1);
+          put_scalar(tag + "_norm2", s2);
+          put_scalar(tag + "_xy", sxy);
+          put_scalar(tag + "_mult_add_s", sec_s);
+          // sample index k: (k * 2654435761 + 12345) mod dim
+          const size_t ns = 4096;
+          vector<double> samp(ns);
+          vector<uint64_t> at(ns);
+          for (size_t k = 0; k < ns; k++) {
+            at[k] = (k * 2654435761ull + 12345ull) % H.dim;
+            samp[k] = y[at[k]];
+          }
+          put(tag + "_at", "u8", {ns}, at.data(), ns);
+          put_d(tag + "_y", samp);
+          uint64_t dim = H.dim;
+          put(tag + "_dim", "u8", {}, &dim, 1);
+        } else {
+          vector<double> alpha, beta, energy;
+          size_t niter = 0;
+          auto t0 = chrono::steady_clock::now();
+          LanczosEigenvalue(H, x0, alpha, beta, energy, niter, true);
+          double sec_s = chrono::duration<double>(chrono::steady_clock::now() - t0).count();
+          put_d(tag + "_alpha", alpha);
+          put_d(tag + "_beta", beta);
+          put_scalar(tag + "_E0", energy[0]);
+          put_scalar(tag + "_seconds", sec_s);
         }
       } else if (cmd == "destroy") {
         string m, secs, tag; int orb, spin, pm; ss >> m >> secs >> orb >> spin >> pm >> tag;

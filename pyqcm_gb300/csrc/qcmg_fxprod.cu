@@ -10,8 +10,10 @@
 //           table serves both.
 //   pass D  one warp per (row band, down state): every down-spin hop adds a
 //           neighbour slab's segment of the band.  Warps sweep the down
-//           states of one band at a time, so the band of x (~48 MB) stays
-//           L2-resident and HBM sees x about once.
+//           states of one band at a time, so the band of x (~26 MB at
+//           L = 16) stays L2-resident and HBM sees x about once; the
+//           gathers run at the L2's throughput, so the kernel is lean in
+//           registers (six blocks per SM) to keep many loads in flight.
 // Restates Hamiltonian_Factorized::mult_add (pyqcm
 // src_ed/Hamiltonian/Hamiltonian_Factorized.hpp:118-170) on fixed-point
 // vectors: hop values share one magnitude per spin (+-t), so a row's hops
@@ -68,9 +70,15 @@ __global__ void __launch_bounds__(512) k_fx_passU(FxProdArgs A) {
 // ---------------------------------------------------------------------------
 // pass U, bulk-copied slabs, grouped ELL hops
 
-// Elements per slab buffer: even (16-byte multiple) and at least du + 2, so
-// the zero slot view[du] lies inside the buffer for either view offset.
-__host__ __device__ inline uint32_t slab_stride(uint32_t du) { return (du + 3u) & ~1u; }
+// Zero slots behind each staged slab: view[du + j] = 0 for j < kZeroSlots,
+// one per bank pair, so padding columns can read a zero from whichever bank
+// pair the real columns of their slot leave free.
+constexpr uint32_t kZeroSlots = 16;
+
+// Elements per slab buffer: even (16-byte multiple) and at least
+// du + 1 + kZeroSlots, so the zero slots lie inside the buffer for either
+// view offset.
+__host__ __device__ inline uint32_t slab_stride(uint32_t du) { return (du + kZeroSlots + 1u + 1u) & ~1u; }
 
 // A slab starts at byte a*du*8, which is 8 mod 16 when du and a are odd.
 // The copy moves the 16-byte-aligned interior [e0, e1); thread 0 loads the
@@ -83,7 +91,7 @@ __device__ __forceinline__ void slab_range(uint32_t a, uint32_t du, uint32_t* e0
 
 // Offset (elements) of the second slab buffer: a compile-time constant, so
 // one address serves the gathers from both slabs.  Two slabs per round need
-// slab_stride(du) <= kSlab1Off (du <= 14205).
+// slab_stride(du) <= kSlab1Off (du <= 14190).
 constexpr uint32_t kSlab1Off = 14208;
 
 // Groups of a row whose columns are requested together before the gathers.
@@ -118,7 +126,7 @@ __device__ __forceinline__ void gather_group(uint32_t vbase, uint2 w, int64_t (&
 // i: one 8-byte load brings four 16-bit hop columns of row i, and each
 // column is gathered from all NS staged slabs.  Row i lists its positive
 // hops in its first groups and its negative hops after them; padding
-// columns point at the zero slot du.  With NS = 2 the grid is even, so the
+// columns point at zero slots du..du+15.  With NS = 2 the grid is even, so the
 // two slabs of a round have the same alignment (view offset).  With NS = 1
 // a second CTA on the SM computes while this one's copy is in flight.
 template <int INTER, int NS, bool FAST>
@@ -189,8 +197,9 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
         const size_t base = (size_t)a * du;
         if (e0 == 1u) v[0] = A.x[base];
         if (e1 == du - 1u) v[du - 1] = A.x[base + du - 1];
-        v[du] = 0;  // zero slot for padding columns
       }
+      if (tid < (int)kZeroSlots && a0 + s * G < dd)
+        smem_slab[s * kSlab1Off + e0 + du + tid] = 0;  // zero slots for padding columns
     }
     __syncthreads();
     const uint32_t vbase = smem_u32(view);
@@ -199,14 +208,23 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
     // columns, diagonal and accumulated input are all requested before its
     // first gather
     uint32_t c_next = tid < du ? __ldg(A.cnt4 + tid) : 0u;
+    // the table holds at least kPreGroups groups per row (zero-slot padding),
+    // so the first ones are loaded and gathered without a per-row test; they
+    // are requested one row ahead, off the gathers' critical path
+    uint2 w_next[kPreGroups];
+#pragma unroll
+    for (int g = 0; g < kPreGroups; ++g)
+      w_next[g] = tid < du ? __ldg(A.ell4 + (size_t)g * du + tid) : make_uint2(0u, 0u);
     for (uint32_t i = tid; i < du; i += bd) {
       const uint32_t c = c_next;
       const uint32_t gp = c & 0xffu, gt = gp + (c >> 8);
-      // the table holds at least kPreGroups groups per row (zero-slot padding),
-      // so the first ones are loaded and gathered without a per-row test
       uint2 w[kPreGroups];
 #pragma unroll
-      for (int g = 0; g < kPreGroups; ++g) w[g] = __ldg(A.ell4 + (size_t)g * du + i);
+      for (int g = 0; g < kPreGroups; ++g) w[g] = w_next[g];
+      if (i + bd < du) {
+#pragma unroll
+        for (int g = 0; g < kPreGroups; ++g) w_next[g] = __ldg(A.ell4 + (size_t)g * du + i + bd);
+      }
       const int64_t dui = FAST ? 0 : __ldg(A.dup + i);
       const int32_t dui32 = FAST ? __ldg(A.dup32 + i) : 0;
       const uint32_t ubits = __ldg(A.bin_up + i);
@@ -286,112 +304,80 @@ __global__ void __launch_bounds__(NS == 1 ? 512 : 1024, NS == 1 ? 2 : 1) k_fx_pa
 }
 
 // ---------------------------------------------------------------------------
-// pass D: one warp per (band, down state)
+// pass D, lean form: one VEC-chunk per lane per sweep (32*VEC rows), so a
+// thread holds few registers and eight 256-thread blocks fit on an SM; the
+// neighbour columns of an item (at most 32 of them in one register per lane)
+// are read once per item, not once per sweep.
 
-// Adds, for the neighbours k in [kf, kt) of the current chunk (columns held
-// one per lane in ccol), the band segments at rows ia.. and ib.. (VEC
-// consecutive elements each) into acc.
-template <int VEC>
-__device__ __forceinline__ void passD_accum(const int64_t* __restrict__ x, uint32_t du,
-                                            uint32_t ccol, uint32_t kf, uint32_t kt, uint32_t ia,
-                                            uint32_t ib, bool va, bool vb, int64_t (&acc)[2 * VEC]) {
+template <int VEC, bool NEG>
+__device__ __forceinline__ void passD5_accum(const int64_t* __restrict__ x, uint32_t du,
+                                             uint32_t ccol, uint32_t kf, uint32_t kt, uint32_t ir,
+                                             int64_t (&acc)[VEC]) {
 #pragma unroll 4
   for (uint32_t k = kf; k < kt; ++k) {
     const uint32_t b = __shfl_sync(0xffffffffu, ccol, (int)k);
-    const int64_t* src = x + (size_t)b * du;
+    const int64_t* src = x + (size_t)b * du + ir;
     if (VEC == 2) {
-      if (va) {
-        const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(src + ia));
-        acc[0] += v.x;
-        acc[1] += v.y;
-      }
-      if (vb) {
-        const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(src + ib));
-        acc[2] += v.x;
-        acc[3] += v.y;
-      }
+      const longlong2 v = __ldcg(reinterpret_cast<const longlong2*>(src));
+      acc[0] += NEG ? -v.x : v.x;
+      acc[VEC - 1] += NEG ? -v.y : v.y;
     } else {
-      if (va) acc[0] += __ldcg(src + ia);
-      if (vb) acc[1] += __ldcg(src + ib);
+      const int64_t v = __ldcg(src);
+      acc[0] += NEG ? -v : v;
     }
   }
 }
 
-// VEC = 2 needs du even (every slab segment at an even row is 16-byte
-// aligned); bands start at multiples of 256 rows.  DOT: also the dot
-// product of the finished y with A.dot_x (the element of x at the same
-// place is in the band of x that L2 holds).
-template <int VEC, bool FAST, bool DOT>
-__global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
+// Items (band, down state) are numbered in 32 bits (launch contract:
+// nbands * dd < 2^32).  A row's hops are summed with their signs into one
+// accumulator per element (exact: |sum| < 2^61).
+template <int VEC, bool FAST, bool DOT, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_fx_passD5(FxProdArgs A) {
   const uint32_t du = A.du, dd = A.dd;
   const uint32_t lane = threadIdx.x & 31u;
-  const size_t warp = ((size_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const size_t nwarps = ((size_t)gridDim.x * blockDim.x) >> 5;
-  const size_t items = (size_t)A.nbands * dd;
-  constexpr uint32_t kSweep = 64u * VEC;  // rows per warp sweep: two VEC-chunks per lane
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t items = A.nbands * dd;
+  constexpr uint32_t kSweep = 32u * VEC;
   I128 dot = {0, 0};
-  for (size_t it = warp; it < items; it += nwarps) {
-    const uint32_t band = (uint32_t)(it / dd), a = (uint32_t)(it % dd);
+  for (uint32_t it = warp; it < items; it += nwarps) {
+    const uint32_t band = it / dd, a = it - band * dd;
     const uint32_t r0 = band * A.band, r1 = min(du, r0 + A.band);
     const uint32_t k0 = A.rp_dn[a], np = A.rs_dn[a] - k0, nt = A.rp_dn[a + 1] - k0;
-    int64_t* yrow = A.y + (size_t)a * du;
     for (uint32_t i0 = r0; i0 < r1; i0 += kSweep) {
-      const uint32_t ia = i0 + lane * VEC, ib = ia + 32u * VEC;
-      const bool va = ia < r1, vb = ib < r1;
-      int64_t P[2 * VEC], N[2 * VEC];
+      const uint32_t ia = i0 + lane * VEC;
+      // lanes past the band's end read a valid row of the band (r0) and drop it
+      const uint32_t ir = ia < r1 ? ia : r0;
+      int64_t acc[VEC];
 #pragma unroll
-      for (int e = 0; e < 2 * VEC; ++e) P[e] = N[e] = 0;
-      for (uint32_t kc = 0; kc < nt; kc += 32u) {
-        const uint32_t ccol = (kc + lane < nt) ? A.col_dn[k0 + kc + lane] : 0u;
+      for (int e = 0; e < VEC; ++e) acc[e] = 0;
+      for (uint32_t kc = 0; kc < nt; kc += 32u) {  // neighbour columns, 32 at a time
+        const uint32_t ccol = (kc + lane < nt) ? __ldg(A.col_dn + k0 + kc + lane) : 0u;
         const uint32_t e = min(32u, nt - kc);
         const uint32_t spos = np > kc ? min(e, np - kc) : 0u;
-        passD_accum<VEC>(A.x, du, ccol, 0u, spos, ia, ib, va, vb, P);
-        passD_accum<VEC>(A.x, du, ccol, spos, e, ia, ib, va, vb, N);
+        passD5_accum<VEC, false>(A.x, du, ccol, 0u, spos, ir, acc);
+        passD5_accum<VEC, true>(A.x, du, ccol, spos, e, ir, acc);
       }
-      // y streams through once (evict-first), leaving L2 to the band of x
+      if (ia >= r1) continue;
+      const size_t at = (size_t)a * du + ia;
       auto term = [&](int64_t v) {
         return FAST ? rshift_fixed(v, A.t_dn, A.r_dn) : mul_fix(v, A.mt_dn, A.sh_dn);
       };
-      const int64_t* xrow = DOT ? A.dot_x + (size_t)a * du : nullptr;
-      auto acc_dot = [&](int64_t yv, int64_t xv) {
-        dot = add128(dot, shr128(mul_s64(yv, xv), kDotShift));
-      };
       if constexpr (VEC == 2) {
-        if (va) {
-          longlong2* yp = reinterpret_cast<longlong2*>(yrow + ia);
-          longlong2 v = __ldcs(yp);
-          v.x += term(P[0] - N[0]);
-          v.y += term(P[1] - N[1]);
-          __stcs(yp, v);
-          if (DOT) {
-            const longlong2 xv = __ldcg(reinterpret_cast<const longlong2*>(xrow + ia));
-            acc_dot(v.x, xv.x);
-            acc_dot(v.y, xv.y);
-          }
-        }
-        if (vb) {
-          longlong2* yp = reinterpret_cast<longlong2*>(yrow + ib);
-          longlong2 v = __ldcs(yp);
-          v.x += term(P[2] - N[2]);
-          v.y += term(P[3] - N[3]);
-          __stcs(yp, v);
-          if (DOT) {
-            const longlong2 xv = __ldcg(reinterpret_cast<const longlong2*>(xrow + ib));
-            acc_dot(v.x, xv.x);
-            acc_dot(v.y, xv.y);
-          }
+        longlong2* yp = reinterpret_cast<longlong2*>(A.y + at);
+        longlong2 v = __ldcs(yp);
+        v.x += term(acc[0]);
+        v.y += term(acc[1]);
+        __stcs(yp, v);
+        if (DOT) {
+          const longlong2 xv = __ldcg(reinterpret_cast<const longlong2*>(A.dot_x + at));
+          dot = add128(dot, shr128(mul_s64(v.x, xv.x), kDotShift));
+          dot = add128(dot, shr128(mul_s64(v.y, xv.y), kDotShift));
         }
       } else {
-        if (va) {
-          const int64_t v = __ldcs(yrow + ia) + term(P[0] - N[0]);
-          __stcs(yrow + ia, v);
-          if (DOT) acc_dot(v, __ldcg(xrow + ia));
-        }
-        if (vb) {
-          const int64_t v = __ldcs(yrow + ib) + term(P[1] - N[1]);
-          __stcs(yrow + ib, v);
-          if (DOT) acc_dot(v, __ldcg(xrow + ib));
-        }
+        const int64_t v = __ldcs(A.y + at) + term(acc[0]);
+        __stcs(A.y + at, v);
+        if (DOT) dot = add128(dot, shr128(mul_s64(v, __ldcg(A.dot_x + at)), kDotShift));
       }
     }
   }
@@ -403,12 +389,12 @@ __global__ void __launch_bounds__(256) k_fx_passD4(FxProdArgs A) {
 
 // Grouped ELL: row i holds ceil(np/4) groups of its positive hop columns,
 // then ceil(nn/4) groups of its negative ones, four 16-bit columns per
-// group, padded with dim (the zero slot behind each staged slab);
+// group, padded with zero slots (dim..dim+15, behind each staged slab);
 // ell4[g * dim + i] is group g of row i and cnt4[i] = positive groups |
 // (negative groups << 8).
 bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const DevBuf<uint32_t>& col,
                 uint32_t dim, cudaStream_t s, DevBuf<uint2>& ell4, DevBuf<uint16_t>& cnt4) {
-  if (dim == 0 || dim > 65534u) return false;
+  if (dim == 0 || dim + kZeroSlots > 65536u) return false;
   std::vector<uint32_t> hrp(dim + 1), hrs(dim);
   QCMG_CUDA(cudaMemcpyAsync(hrp.data(), rp.p, (dim + 1) * 4, cudaMemcpyDeviceToHost, s));
   QCMG_CUDA(cudaMemcpyAsync(hrs.data(), rs.p, dim * 4, cudaMemcpyDeviceToHost, s));
@@ -431,63 +417,89 @@ bool build_ell4(const DevBuf<uint32_t>& rp, const DevBuf<uint32_t>& rs, const De
   // position k%4) is gathered by 16 lanes at once: the rows of one
   // half-warp, 16 consecutive rows from a multiple of 16.  An 8-byte shared
   // load costs one wavefront per distinct address on its busiest bank pair
-  // (column mod 16), and a row's columns may take any order within its
-  // positive and its negative list.  So, slot by slot, each row of a
-  // half-warp takes the remaining column of the slot's sign list whose bank
-  // pair is least used so far in that slot; rows with the fewest choices go
-  // first.  On the 4x4 half bases this cuts the wavefronts from ~1.8x to
-  // ~1.55x the conflict-free count.
+  // (column mod 16).  A row's columns may take any order within its positive
+  // and its negative slot range, and a row may read a zero slot (one per
+  // bank pair) in any slot of its range that it does not need.  So, slot by
+  // slot, rows are matched to distinct bank pairs (a maximum bipartite
+  // matching by augmenting paths, rows whose remaining columns leave them the
+  // least slack first); an unmatched row with no slack left takes a column
+  // anyway (a conflict), and the others read the zero slot of a bank pair
+  // the slot leaves free.  On the 4x4 half bases this brings the wavefronts
+  // from ~1.55x to ~1.06x the slot count (a per-slot greedy choice of the
+  // least-used bank pair got ~1.55x).
   for (uint32_t i = 0; i < dim; ++i) {
     const uint32_t np = hrs[i] - hrp[i], nn = hrp[i + 1] - hrs[i];
     hc[i] = (uint16_t)(((np + 3) / 4) | (((nn + 3) / 4) << 8));
   }
+  // the zero slot on bank pair p
+  auto zero_on = [&](uint32_t p) { return (uint16_t)(dim + (p + 16u - dim % 16u) % 16u); };
   std::vector<std::vector<uint32_t>> remp(16), remn(16);
-  std::vector<uint32_t> order;
+  std::vector<uint32_t>* lst[16] = {};
+  uint32_t order[16];
+  double slack[16];
+  int owner[16], choice[16];
+  auto augment = [&](auto&& self, int r, uint32_t& seen) -> bool {
+    for (uint32_t c : *lst[r]) {
+      const uint32_t b = c % 16u;
+      if ((seen >> b) & 1u) continue;
+      seen |= 1u << b;
+      if (owner[b] < 0 || self(self, owner[b], seen)) {
+        owner[b] = r;
+        choice[r] = (int)c;
+        return true;
+      }
+    }
+    return false;
+  };
   for (uint32_t b0 = 0; b0 < dim; b0 += 16) {
     const uint32_t nr = std::min<uint32_t>(16, dim - b0);
-    uint32_t kmax = 0;
+    uint32_t kmax = 4u * kPreGroups;
     for (uint32_t r = 0; r < nr; ++r) {
       const uint32_t i = b0 + r;
       remp[r].assign(hcol.begin() + hrp[i], hcol.begin() + hrs[i]);
       remn[r].assign(hcol.begin() + hrs[i], hcol.begin() + hrp[i + 1]);
-      std::sort(remp[r].begin(), remp[r].end());
-      std::sort(remn[r].begin(), remn[r].end());
       kmax = std::max<uint32_t>(kmax, 4u * ((hc[i] & 0xffu) + (hc[i] >> 8)));
     }
     for (uint32_t k = 0; k < kmax; ++k) {
-      // the list slot k draws from, for row r (null: padding)
-      auto list = [&](uint32_t r) -> std::vector<uint32_t>* {
+      uint32_t nl = 0;
+      for (uint32_t r = 0; r < nr; ++r) {
         const uint32_t c = hc[b0 + r], gp = c & 0xffu, gt = gp + (c >> 8);
-        if (k < 4 * gp) return &remp[r];
-        if (k < 4 * gt) return &remn[r];
-        return nullptr;
-      };
-      order.resize(nr);
-      for (uint32_t r = 0; r < nr; ++r) order[r] = r;
-      std::stable_sort(order.begin(), order.end(), [&](uint32_t p, uint32_t q) {
-        const std::vector<uint32_t>* lp = list(p);
-        const std::vector<uint32_t>* lq = list(q);
-        const size_t np = (lp && !lp->empty()) ? lp->size() : SIZE_MAX;
-        const size_t nq = (lq && !lq->empty()) ? lq->size() : SIZE_MAX;
-        return np < nq;
-      });
-      uint32_t used[16] = {0};
-      bool zero_used = false;
-      for (uint32_t r : order) {
-        std::vector<uint32_t>* l = list(r);
-        uint32_t j = Z;
-        if (l && !l->empty()) {
-          size_t best = 0;
-          for (size_t q = 1; q < l->size(); ++q)
-            if (used[(*l)[q] % 16] < used[(*l)[best] % 16]) best = q;
-          j = (*l)[best];
-          l->erase(l->begin() + best);
-          ++used[j % 16];
-        } else if (!zero_used) {  // padding: every padded lane reads the same zero slot
-          zero_used = true;
-          ++used[Z % 16];
+        lst[r] = nullptr;
+        if (k < 4 * gp) {
+          lst[r] = &remp[r];
+          slack[r] = (double)(4 * gp - k) - (double)remp[r].size();
+        } else if (k < 4 * gt) {
+          lst[r] = &remn[r];
+          slack[r] = (double)(4 * gt - k) - (double)remn[r].size();
         }
-        cols[((size_t)(k / 4) * dim + b0 + r) * 4 + (k % 4)] = (uint16_t)j;
+        if (lst[r] && lst[r]->empty()) lst[r] = nullptr;
+        choice[r] = -1;
+        if (lst[r]) order[nl++] = r;
+      }
+      std::stable_sort(order, order + nl, [&](uint32_t p, uint32_t q) { return slack[p] < slack[q]; });
+      for (int b = 0; b < 16; ++b) owner[b] = -1;
+      for (uint32_t q = 0; q < nl; ++q) {
+        uint32_t seen = 0;
+        augment(augment, (int)order[q], seen);
+      }
+      uint32_t used = 0;
+      for (uint32_t r = 0; r < nr; ++r) {
+        if (!lst[r]) continue;
+        if (choice[r] < 0 && slack[r] > 0.5) continue;  // pads this slot, places later
+        const uint32_t c = choice[r] >= 0 ? (uint32_t)choice[r] : lst[r]->front();
+        lst[r]->erase(std::find(lst[r]->begin(), lst[r]->end(), c));
+        used |= 1u << (c % 16u);
+        cols[((size_t)(k / 4) * dim + b0 + r) * 4 + (k % 4)] = (uint16_t)c;
+        choice[r] = (int)c;
+      }
+      // padding lanes of this slot read one zero slot, on a bank pair the slot
+      // leaves free when there is one
+      uint32_t p = (uint32_t)__builtin_ctz(~used | 0x10000u) & 15u;
+      const uint16_t zp = zero_on(p);
+      for (uint32_t r = 0; r < nr; ++r) {
+        const uint32_t c = hc[b0 + r], gt = (c & 0xffu) + (c >> 8);
+        const bool active = k < 4u * std::max<uint32_t>(gt, kPreGroups);
+        if (active && choice[r] < 0) cols[((size_t)(k / 4) * dim + b0 + r) * 4 + (k % 4)] = zp;
       }
     }
   }
@@ -512,7 +524,7 @@ int pow2_exponent(int64_t m) {
 }
 
 int choose_slabs_per_pass(uint32_t du, int max_optin_smem) {
-  if (du < 64 || du > 65534u) return 0;
+  if (du < 64 || du + kZeroSlots > 65536u) return 0;
   const size_t one = (size_t)slab_stride(du) * 8;
   if (one > (size_t)max_optin_smem) return 0;
   const bool two_fit = slab_stride(du) <= kSlab1Off &&
@@ -588,19 +600,25 @@ unsigned launch_product(const qcmg_hamiltonian* H, const FxProdArgs& A, cudaStre
   QCMG_CUDA(cudaGetLastError());
   // pass D
   const size_t items = (size_t)A.nbands * H->dd;
-  const unsigned gD = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * 8));
-  auto passD = [&](auto vec_tag, auto fast_tag) {
-    constexpr int V = decltype(vec_tag)::value;
-    constexpr bool F = decltype(fast_tag)::value;
-    if (A.dot_part) k_fx_passD4<V, F, true><<<gD, 256, 0, s>>>(A);
-    else k_fx_passD4<V, F, false><<<gD, 256, 0, s>>>(A);
+  if (items >= (1ull << 32)) throw Error(QCMG_ERR_ARG, "sector too large for pass D's 32-bit item numbers");
+  auto go = [&](auto kern) {
+    int per_sm = 0;
+    QCMG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 256, 0));
+    per_sm = std::max(1, std::min(per_sm, 8));  // dot partials: at most 8 blocks per SM
+    const unsigned g = (unsigned)std::max<size_t>(1, std::min<size_t>((items + 7) / 8, (size_t)sms * per_sm));
+    kern<<<g, 256, 0, s>>>(A);
+    return g;
   };
-  if ((H->du & 1u) == 0u) {
-    if (fast) passD(Two{}, Fast{});
-    else passD(Two{}, Full{});
+  // six 256-thread blocks per SM (40 registers) for the product; five for
+  // the Lanczos form, whose 128-bit dot accumulator needs the registers
+  const bool even = (H->du & 1u) == 0u;
+  unsigned gD;
+  if (A.dot_part) {
+    if (even) gD = fast ? go(k_fx_passD5<2, true, true, 5>) : go(k_fx_passD5<2, false, true, 5>);
+    else gD = fast ? go(k_fx_passD5<1, true, true, 5>) : go(k_fx_passD5<1, false, true, 5>);
   } else {
-    if (fast) passD(One{}, Fast{});
-    else passD(One{}, Full{});
+    if (even) gD = fast ? go(k_fx_passD5<2, true, false, 6>) : go(k_fx_passD5<2, false, false, 6>);
+    else gD = fast ? go(k_fx_passD5<1, true, false, 6>) : go(k_fx_passD5<1, false, false, 6>);
   }
   QCMG_CUDA(cudaGetLastError());
   return gD;
