@@ -365,12 +365,13 @@ def run_lanczos(args):
 
 
 def _vca_3x4():
-    """3x4 cluster, t=1 t'=-0.3 U=8 mu=4, AF Weiss field M (configs' VCA case)."""
+    """3x4 cluster, t=1 t'=-0.3 U=8 mu=4, AF Weiss field M (the VCA case)."""
     import pyqcm_gb300 as pg
     from pyqcm_gb300.lattice import LatticeModel
     cm = pg.ClusterModel(12, 0)
     sites = [(x, y, 0) for y in range(3) for x in range(4)]
-    lm = LatticeModel(cm, sites, [(4, 0, 0), (0, 3, 0)])
+    # superlattice (4,0), (1,3): the Neel wavevector is commensurate with it
+    lm = LatticeModel(cm, sites, [(4, 0, 0), (1, 3, 0)])
     lm.interaction_operator("U", 1.0)
     lm.hopping_operator("t", (1, 0, 0), -1.0)
     lm.hopping_operator("t", (0, 1, 0), -1.0)

@@ -327,19 +327,25 @@ def run_many(loops, workers=4):
         return list(ex.map(one, loops))
 
 
-def plaquette_bath_model(n_bath=8, sector="R0:N12:S0"):
-    """The 2x2 plaquette with n_bath bath orbitals on the square lattice
-    (bath k: energy eb{k+1}, hybridization tb{k+1} with site k % 4), with
+def plaquette_bath_model(n_bath=8, sector="R0:N12:S0", hybridizations=1):
+    """The 2x2 plaquette with n_bath bath orbitals on the square lattice, with
     lattice operators t (nearest neighbour), tp (diagonal), U and the built-in
-    mu: the batched-CDMFT benchmark model, with one hybridization per bath
-    orbital."""
+    mu.  Bath k has energy eb{k+1} and hybridization tb{k+1} with site k % 4;
+    with hybridizations=2 it also couples to site (k+1) % 4 through
+    tb{k+1+n_bath} (8 energies + 16 hybridizations for 8 baths: the
+    batched-CDMFT configuration)."""
     from .lattice import LatticeModel
+    if hybridizations not in (1, 2):
+        raise ValueError("hybridizations must be 1 or 2")
     ns, no = 4, 4 + n_bath
     cm = ClusterModel(ns, n_bath)
     for k in range(n_bath):
         b, s = ns + k, k % ns
         cm.new_operator(f"eb{k+1}", "one-body", [(b, b, 1.0), (b + no, b + no, 1.0)])
         cm.new_operator(f"tb{k+1}", "one-body", [(s, b, 1.0), (s + no, b + no, 1.0)])
+        if hybridizations == 2:
+            s2 = (k + 1) % ns
+            cm.new_operator(f"tb{k+1+n_bath}", "one-body", [(s2, b, 1.0), (s2 + no, b + no, 1.0)])
     lm = LatticeModel(cm, [(0, 0, 0), (1, 0, 0), (0, 1, 0), (1, 1, 0)], [(2, 0, 0), (0, 2, 0)])
     lm.interaction_operator("U", 1.0)
     lm.hopping_operator("t", (1, 0, 0), -1.0)
@@ -350,6 +356,7 @@ def plaquette_bath_model(n_bath=8, sector="R0:N12:S0"):
     return lm
 
 
-def bath_names(n_bath):
+def bath_names(n_bath, hybridizations=1):
     """Lattice-level names of the bath parameters of plaquette_bath_model."""
-    return [f"eb{k+1}_1" for k in range(n_bath)] + [f"tb{k+1}_1" for k in range(n_bath)]
+    return ([f"eb{k+1}_1" for k in range(n_bath)]
+            + [f"tb{k+1}_1" for k in range(hybridizations * n_bath)])

@@ -164,7 +164,9 @@ def _lattice_head(ns, nb, bath_ops, sites, superlattice, ops, params, sector):
 
 def bench_c2():
     """The VCA case on its benchmarked grid: 3x4 cluster (4 wide, 3 high),
-    t=1, t'=-0.3, U=8, mu=4, Neel Weiss field M_1=0.1; ground-state energy,
+    tiled by the superlattice (4,0), (1,3) on which the Neel wavevector is
+    commensurate (the reference refuses (4,0), (0,3) for a density wave at
+    (pi, pi)), t=1, t'=-0.3, U=8, mu=4, Neel Weiss field M_1=0.1; ground-state energy,
     both spin blocks' Q-matrices, the cluster part of Omega and the Potthoff
     functional on the 128x128 wavevector grid x 256 Gauss-Legendre
     frequencies (reference: QCM::Potthoff_functional, grid path)."""
@@ -174,7 +176,7 @@ def bench_c2():
            ("hop", "t", (0, 1, 0), -1.0, 1, 0), ("hop", "tp", (1, 1, 0), -1.0, 1, 0),
            ("hop", "tp", (-1, 1, 0), -1.0, 1, 0), ("dw", "M", "Z", (1, 1, 0), 1.0, 0.0)]
     params = {"t": 1.0, "tp": -0.3, "U": 8.0, "mu": 4.0, "M": 0.0, "M_1": 0.1}
-    lines = _lattice_head(12, 0, None, sites, [(4, 0, 0), (0, 3, 0)], ops, params, "R0:N12:S0")
+    lines = _lattice_head(12, 0, None, sites, [(4, 0, 0), (1, 3, 0)], ops, params, "R0:N12:S0")
     w, wt = legendre_frequency_grid(1.0, 10.0, 64, 128, 64)
     lines += ["gs 0 gs", "qmatrix 0 0 qup", "qmatrix 0 1 qdn", "omega 0 omega_clus",
               "lat_kgrid 128 128 1",
