@@ -170,15 +170,27 @@ int qcmg_seeded_vector(size_t dim, unsigned seed, double* out);
  * residual |s_last * beta| < tol or after max_iter steps.  With reorth > 0 the
  * Lanczos basis is kept on the device and every new vector is
  * reorthogonalized (classical Gram-Schmidt, twice) against all previous ones;
- * at most `reorth` vectors are kept.
+ * at most `reorth` vectors are kept: when that many are held and the residual
+ * has not converged, the iteration restarts from the current Ritz vector.
  * Outputs: *E0; psi (length dim, may be NULL: then no second pass);
- * *niter; alpha, beta (capacity `cap`, may be NULL).
+ * *niter (all iterations, restarts included); alpha, beta (capacity `cap`,
+ * may be NULL: the coefficients of the last restart cycle).
  * Replaces LanczosEigenvalue + LanczosEigenvector
  * (src_ed/Hamiltonian/Lanczos.hpp:41-143) as called from
  * Hamiltonian::states (src_ed/Hamiltonian/Hamiltonian_base.hpp:114-221). */
 int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned seed, double tol,
                               int max_iter, int reorth, double* E0, double* psi, int* niter,
                               double* alpha, double* beta, int cap);
+
+/* Breakdown of the last reorthogonalized qcmg_lanczos_ground_state on H:
+ * device time of the products and of the Gram-Schmidt sweeps (ms), the
+ * sweeps' algorithmic bytes (16 per stored vector element per pass, two
+ * passes per step), restarts, vectors held at most, and the length of the
+ * last restart cycle (the number of alpha/beta coefficients returned).  Any
+ * pointer may be NULL.  No counterpart in the reference, whose Lanczos has no
+ * reorthogonalization (src_ed/Hamiltonian/Lanczos.hpp:41-95). */
+int qcmg_lanczos_last_stats(qcmg_hamiltonian* H, double* product_ms, double* reorth_ms,
+                            double* reorth_bytes, int* restarts, int* vectors, int* cycle);
 
 /* Band Lanczos from p start vectors phi (p x dim, row-major: vector k at
  * phi + k*dim).  M_target is the requested number of steps (the reference

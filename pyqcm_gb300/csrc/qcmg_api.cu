@@ -440,10 +440,31 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
     LanczosResult r = lanczos_ground_state(H, x0, seed, tol, max_iter, reorth, psi);
     *E0 = r.energy;
     if (niter) *niter = r.niter;
-    for (int k = 0; k < std::min<int>(cap, r.niter); ++k) {
+    const int nc = (int)r.alpha.size();  // the last cycle's coefficients
+    for (int k = 0; k < std::min<int>(cap, nc); ++k) {
       if (alpha) alpha[k] = r.alpha[k];
       if (beta) beta[k] = r.beta[k];
     }
+    H->last_product_ms = r.product_ms;
+    H->last_reorth_ms = r.reorth_ms;
+    H->last_reorth_bytes = r.reorth_bytes;
+    H->last_restarts = r.restarts;
+    H->last_vectors = r.vectors;
+    H->last_cycle = nc;
+  });
+}
+
+int qcmg_lanczos_last_stats(qcmg_hamiltonian* H, double* product_ms, double* reorth_ms,
+                            double* reorth_bytes, int* restarts, int* vectors, int* cycle) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr, "NULL handle");
+    std::lock_guard<std::mutex> lock(H->mu);
+    if (product_ms) *product_ms = H->last_product_ms;
+    if (reorth_ms) *reorth_ms = H->last_reorth_ms;
+    if (reorth_bytes) *reorth_bytes = H->last_reorth_bytes;
+    if (restarts) *restarts = H->last_restarts;
+    if (vectors) *vectors = H->last_vectors;
+    if (cycle) *cycle = H->last_cycle;
   });
 }
 

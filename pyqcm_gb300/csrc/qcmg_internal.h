@@ -169,6 +169,9 @@ struct qcmg_hamiltonian {
   qcmg::DevBuf<double> scalars;
   qcmg::FxTables fx;
   int use_fx = 1;  // 1: fixed-point fast path when applicable; 0: FP64 kernels
+  // breakdown of the last reorthogonalized Lanczos solve on this handle
+  double last_product_ms = 0.0, last_reorth_ms = 0.0, last_reorth_bytes = 0.0;
+  int last_restarts = 0, last_vectors = 0, last_cycle = 0;
   std::mutex mu;   // serializes calls on one handle
 };
 

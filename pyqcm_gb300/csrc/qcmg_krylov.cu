@@ -369,6 +369,24 @@ struct DevVec {
   }
 };
 
+// CUDA events for the per-solve device-time breakdown.
+struct Events {
+  cudaEvent_t e[4] = {nullptr, nullptr, nullptr, nullptr};
+  Events() {
+    for (auto& x : e) QCMG_CUDA(cudaEventCreate(&x));
+  }
+  ~Events() {
+    for (auto& x : e)
+      if (x) cudaEventDestroy(x);
+  }
+  void record(int k, cudaStream_t s) { QCMG_CUDA(cudaEventRecord(e[k], s)); }
+  double elapsed(int a, int b) const {  // both recorded and complete
+    float ms = 0.0f;
+    QCMG_CUDA(cudaEventElapsedTime(&ms, e[a], e[b]));
+    return ms;
+  }
+};
+
 LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, unsigned seed,
                                    double tol, int max_iter, int reorth, double* psi_host) {
   const size_t n = H->dim;
@@ -452,42 +470,85 @@ LanczosResult lanczos_ground_state(qcmg_hamiltonian* H, const double* x0_host, u
   }
 
   // Fully reorthogonalized Lanczos: the basis is kept in HBM and every new
-  // residual is projected out of it twice (classical Gram-Schmidt x2).
-  std::vector<DevVec> V;
+  // residual is projected out of it twice (classical Gram-Schmidt x2).  At
+  // most `reorth` vectors are kept: when the cap is reached before the Ritz
+  // residual converges, the iteration restarts from the current Ritz vector
+  // (explicit restart).  The product is the fixed-point one where it applies
+  // (the vectors stay FP64).  Device time of the products and of the
+  // reorthogonalization is recorded with events (qcmg_lanczos_last_stats).
+  const bool fx = H->use_fx && fx_prepare(H);
+  auto product = [&](const double* x, double* y) {
+    if (fx)
+      fx_matvec_f64(H, x, y, false);
+    else
+      matvec(H, x, y, false);
+  };
+  const int keep = std::max(reorth, 2);
+  std::vector<DevVec> V;  // pool, reused across restarts
   std::vector<const double*> Vp;
   MultiOps mops;
   std::vector<double> c;
   V.emplace_back(n);
   QCMG_CUDA(cudaMemcpyAsync(V[0].p, x0_dev, n * 8, cudaMemcpyDeviceToDevice, s));
-  Vp.push_back(V[0].p);
   double* w = r.p;  // residual
-  double ritz = 2.0 * tol;
-  for (int j = 0; ritz > tol; ++j) {
-    matvec(H, V[j].p, w, false);
-    if (j > 0) axpy(w, V[j - 1].p, -res.beta.back(), n, s);
-    double a = red.dot(V[j].p, w, n, s);
-    res.alpha.push_back(a);
-    axpy(w, V[j].p, -a, n, s);
-    for (int pass = 0; pass < 2; ++pass) {
-      mops.multidot(Vp, w, n, s, c);
-      mops.multiaxpy(Vp, c, w, n, s);
+  Events ev;
+  int total = 0;
+  bool converged = false;
+  while (!converged) {
+    Vp.assign(1, V[0].p);
+    res.alpha.clear();
+    res.beta.clear();
+    for (int j = 0;; ++j) {
+      ev.record(0, s);
+      product(V[j].p, w);
+      ev.record(1, s);
+      if (j > 0) axpy(w, V[j - 1].p, -res.beta.back(), n, s);
+      double a = red.dot(V[j].p, w, n, s);
+      res.alpha.push_back(a);
+      axpy(w, V[j].p, -a, n, s);
+      ev.record(2, s);
+      for (int pass = 0; pass < 2; ++pass) {
+        mops.multidot(Vp, w, n, s, c);
+        mops.multiaxpy(Vp, c, w, n, s);
+      }
+      ev.record(3, s);
+      double b = std::sqrt(red.dot(w, w, n, s));  // synchronizes the stream
+      res.product_ms += ev.elapsed(0, 1);
+      res.reorth_ms += ev.elapsed(2, 3);
+      res.reorth_bytes += 2.0 * 16.0 * (double)Vp.size() * (double)n;  // 16 B per stored element per pass
+      res.beta.push_back(b);
+      ++total;
+      res.energy = tridiag_lowest(res.alpha, res.beta, z);
+      const double ritz = std::fabs(z.back() * b);
+      if (!std::isfinite(res.energy) || !std::isfinite(ritz))
+        throw Error(QCMG_ERR_NUMERIC, "Lanczos produced a non-finite value");
+      if (ritz <= tol || b == 0.0) {
+        converged = true;
+        break;
+      }
+      if (total >= max_iter)
+        throw Error(QCMG_ERR_NOCONV, "reorthogonalized Lanczos did not converge within " +
+                                         std::to_string(max_iter) + " iterations");
+      if ((int)Vp.size() >= keep) break;  // cap reached: restart
+      if ((int)V.size() <= j + 1) V.emplace_back(n);
+      QCMG_CUDA(cudaMemcpyAsync(V[j + 1].p, w, n * 8, cudaMemcpyDeviceToDevice, s));
+      scale(V[j + 1].p, 1.0 / b, n, s);
+      Vp.push_back(V[j + 1].p);
     }
-    double b = std::sqrt(red.dot(w, w, n, s));
-    res.beta.push_back(b);
-    res.energy = tridiag_lowest(res.alpha, res.beta, z);
-    ritz = std::fabs(z.back() * b);
-    if (!std::isfinite(res.energy) || !std::isfinite(ritz))
-      throw Error(QCMG_ERR_NUMERIC, "Lanczos produced a non-finite value");
-    if (ritz <= tol || b == 0.0) break;
-    if ((int)V.size() >= reorth || j + 1 >= max_iter)
-      throw Error(QCMG_ERR_NOCONV, "reorthogonalized Lanczos did not converge within " +
-                                       std::to_string(V.size()) + " stored vectors");
-    V.emplace_back(n);
-    QCMG_CUDA(cudaMemcpyAsync(V.back().p, w, n * 8, cudaMemcpyDeviceToDevice, s));
-    scale(V.back().p, 1.0 / b, n, s);
-    Vp.push_back(V.back().p);
+    if (converged) break;
+    // restart from the Ritz vector sum_k z_k V_k, normalized
+    QCMG_CUDA(cudaMemsetAsync(w, 0, n * 8, s));
+    std::vector<double> mz(z.size());
+    for (size_t k = 0; k < z.size(); ++k) mz[k] = -z[k];
+    mops.multiaxpy(Vp, mz, w, n, s);
+    const double nrm = std::sqrt(red.dot(w, w, n, s));
+    if (!(nrm > 0.0)) throw Error(QCMG_ERR_NUMERIC, "Lanczos restart vector vanished");
+    QCMG_CUDA(cudaMemcpyAsync(V[0].p, w, n * 8, cudaMemcpyDeviceToDevice, s));
+    scale(V[0].p, 1.0 / nrm, n, s);
+    ++res.restarts;
   }
-  res.niter = (int)res.alpha.size();
+  res.niter = total;
+  res.vectors = (int)V.size();
   if (psi_host) {
     DevVec gs(n);
     QCMG_CUDA(cudaMemsetAsync(gs.p, 0, n * 8, s));

@@ -11,6 +11,11 @@ struct LanczosResult {
   std::vector<double> alpha, beta;
   double energy = 0.0;
   int niter = 0;
+  // reorthogonalized solves: device time of the products and of the
+  // Gram-Schmidt sweeps, their algorithmic bytes (16 per stored element per
+  // pass), restarts and the vectors held
+  double product_ms = 0.0, reorth_ms = 0.0, reorth_bytes = 0.0;
+  int restarts = 0, vectors = 0;
 };
 
 struct BandResult {

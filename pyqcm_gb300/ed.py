@@ -233,7 +233,19 @@ class Hamiltonian:
                                               reorth, e0, ptr(psi), nit, ptr(alpha), ptr(beta),
                                               cap))
         n = nit.value
+        if reorth:  # restarted runs return the last cycle's coefficients
+            n = self.lanczos_stats()["cycle"]
         return e0.value, psi, alpha[:n], beta[:n]
+
+    def lanczos_stats(self):
+        """Breakdown of the last reorthogonalized lanczos() on this sector:
+        device ms of the products and of the Gram-Schmidt sweeps, the sweeps'
+        algorithmic bytes, restarts, vectors held, last cycle length."""
+        pm, rm, rb = _lib.c_double(), _lib.c_double(), _lib.c_double()
+        rs, nv, cy = _lib.c_int(), _lib.c_int(), _lib.c_int()
+        check(lib().qcmg_lanczos_last_stats(self._h, pm, rm, rb, rs, nv, cy))
+        return {"product_ms": pm.value, "reorth_ms": rm.value, "reorth_bytes": rb.value,
+                "restarts": rs.value, "vectors": nv.value, "cycle": cy.value}
 
     def GS_energy(self):
         return self.lanczos(want_psi=False)[0]

@@ -109,6 +109,20 @@ def test_large_sector_lanczos_energy(pg, tag, path):
     assert np.max(np.abs(alpha[:n] - g["lz_alpha"][:n])) < 1e-9
 
 
+def test_large_4x4_reorthogonalized_lanczos(pg):
+    """Full reorthogonalization on the 4x4 half-filled sector with at most
+    150 vectors held in HBM (restarting from the Ritz vector at the cap):
+    the energy matches the reference's LanczosEigenvalue to 1e-10."""
+    g = _golden_or_skip("large_4x4")
+    nx, ny, params, sec = LARGE["large_4x4"]
+    H = _hamiltonian(pg, nx, ny, params, sec)
+    e0, _, _, _ = H.lanczos(tol=1e-10, max_iter=1000, reorth=150, want_psi=False)
+    ref = float(g["lz_E0"])
+    assert abs(e0 - ref) <= 1e-10 * abs(ref), (e0, ref)
+    st = H.lanczos_stats()
+    assert st["vectors"] <= 150 and st["reorth_ms"] > 0.0
+
+
 def test_cdmft_plaquette_8bath(pg):
     """Batched-CDMFT model at one parameter point against the reference's ED
     and QCM layers (64x64 k grid, 200 Matsubara frequencies)."""
