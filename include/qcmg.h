@@ -150,12 +150,16 @@ int qcmg_multidot(int m, const double* const* V, const double* w, size_t n, doub
  * framework owning the GPU through its own pool or a memory cap; code that
  * must not allocate while other work runs).  No counterpart in the
  * reference.  Same arguments and kernels, except that out is a DEVICE array
- * of m doubles and the call returns without waiting.  Allocates nothing:
- * the partial sums live in a fixed 155,648-byte device array of the library,
- * so m is limited to 64 (QCMG_ERR_ARG beyond).  The first call on a device
- * (with that device current) looks up that array's address; make it before
- * any stream capture.  Calls that overlap in time on one device race on the
- * array: serialize them. */
+ * of m doubles, the call returns without waiting, and it runs on the calling
+ * thread's current CUDA device (not the one chosen with qcmg_set_device).
+ * Allocates nothing: the partial sums live in a fixed 155,648-byte device
+ * array of the library, so m is limited to 64 (QCMG_ERR_ARG beyond; m == 0
+ * returns QCMG_OK).  The array is reserved when CUDA loads the library's
+ * module on the device, which under lazy module loading (the default) is the
+ * first call: make that first call before handing the GPU's memory to a
+ * pool or a cap, and before any stream capture (it also looks up the
+ * array's address, once per device and context).  Calls that overlap in
+ * time on one device race on the array: serialize them. */
 int qcmg_multidot_noalloc(int m, const double* const* V, const double* w, size_t n, double* out,
                           void* stream);
 
@@ -232,6 +236,15 @@ int qcmg_lanczos_green(qcmg_hamiltonian* H, const double* psi, unsigned flags, d
 int qcmg_block_lanczos(qcmg_hamiltonian* H, int p, const double* phi, unsigned flags,
                        int M_target, int max_iter, double acc_deflation, double acc_band, int* M,
                        int* p_actual, double* A, double* B, double* W, int cap);
+
+/* qcmg_band_lanczos with the p host start vectors given as an array of
+ * pointers (phi[k] of length dim), as the reference holds them
+ * (vector<vector<HF>>& phi of Hamiltonian::build_Q_matrix,
+ * src_ed/Hamiltonian/Hamiltonian_base.hpp:229-254): each is copied to the
+ * device directly, with no flat host copy. */
+int qcmg_band_lanczos_ptrs(qcmg_hamiltonian* H, int p, const double* const* phi, int M_target,
+                           int max_iter, double acc_deflation, double acc_band, int* M,
+                           double* evals, double* Q, int cap);
 
 /* qcmg_band_lanczos with the start vectors already in the handle's device
  * memory (p x dim, row-major; e.g. written there by qcmg_apply_c with

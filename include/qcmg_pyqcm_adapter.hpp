@@ -102,16 +102,16 @@ class Hamiltonian_GPU : public Hamiltonian<HilbertField> {
   Q_matrix<HilbertField> build_Q_matrix(vector<vector<HilbertField>>& phi) override {
     const int p = (int)phi.size();
     if (this->dim == 0 || p == 0) return Q_matrix<HilbertField>(0, 0);
-    std::vector<double> flat((size_t)p * this->dim);
-    for (int k = 0; k < p; ++k)
-      std::copy(phi[k].begin(), phi[k].end(), flat.begin() + (size_t)k * this->dim);
+    std::vector<const double*> ptrs(p);
+    for (int k = 0; k < p; ++k) ptrs[k] = (const double*)phi[k].data();
     const int M = (int)(14 * p * std::log(1.0 * this->dim));
     const int maxit = (int)global_int("max_iter_BL");
     const int cap = maxit + 2 * p + 2;
     std::vector<double> ev(cap), Q((size_t)p * cap);
     int Mo = 0;
-    check(qcmg_band_lanczos(H_, p, flat.data(), M, maxit, global_double("accur_deflation"),
-                            global_double("accur_band_lanczos"), &Mo, ev.data(), Q.data(), cap));
+    check(qcmg_band_lanczos_ptrs(H_, p, ptrs.data(), M, maxit, global_double("accur_deflation"),
+                                 global_double("accur_band_lanczos"), &Mo, ev.data(), Q.data(),
+                                 cap));
     Q_matrix<HilbertField> out(p, Mo);
     for (int i = 0; i < Mo; ++i) out.e[i] = ev[i];
     for (int a = 0; a < p; ++a)

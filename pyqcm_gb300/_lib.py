@@ -60,6 +60,8 @@ SIGNATURES = {
     "qcmg_lanczos_last_stats": (c_int, [vp, dbl_p, dbl_p, dbl_p, int_p, int_p, int_p]),
     "qcmg_band_lanczos": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p, vp,
                                   vp, c_int]),
+    "qcmg_band_lanczos_ptrs": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p,
+                                       vp, vp, c_int]),
     "qcmg_band_lanczos_device": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p,
                                          vp, vp, c_int]),
     "qcmg_lanczos_green": (c_int, [vp, vp, c_uint, c_double, c_int, int_p, vp, vp, c_int]),

@@ -537,6 +537,34 @@ int qcmg_band_lanczos(qcmg_hamiltonian* H, int p, const double* phi, int M_targe
                             evals, Q, cap);
 }
 
+int qcmg_band_lanczos_ptrs(qcmg_hamiltonian* H, int p, const double* const* phi, int M_target,
+                           int max_iter, double acc_deflation, double acc_band, int* M,
+                           double* evals, double* Q, int cap) {
+  // each host vector goes straight to its row of one device block
+  DevBuf<double> dev;
+  const int rc = guarded([&] {
+    QCMG_CHECK_ARG(H != nullptr && phi != nullptr && M != nullptr, "NULL argument");
+    QCMG_CHECK_ARG(p > 0, "invalid band Lanczos sizes");
+    std::lock_guard<std::mutex> lock(H->mu);
+    QCMG_CUDA(cudaSetDevice(H->device));
+    if (H->dim == 0) return;
+    dev.alloc((size_t)p * H->dim);
+    for (int k = 0; k < p; ++k) {
+      QCMG_CHECK_ARG(phi[k] != nullptr, "NULL start vector");
+      QCMG_CUDA(cudaMemcpyAsync(dev.p + (size_t)k * H->dim, phi[k], H->dim * 8,
+                                cudaMemcpyHostToDevice, H->stream));
+    }
+    QCMG_CUDA(cudaStreamSynchronize(H->stream));
+  });
+  if (rc != QCMG_OK) return rc;
+  if (H->dim == 0) {
+    *M = 0;
+    return QCMG_OK;
+  }
+  return band_lanczos_entry(H, p, dev.p, true, M_target, max_iter, acc_deflation, acc_band, M,
+                            evals, Q, cap);
+}
+
 int qcmg_band_lanczos_device(qcmg_hamiltonian* H, int p, const double* phi_dev, int M_target,
                              int max_iter, double acc_deflation, double acc_band, int* M,
                              double* evals, double* Q, int cap) {
