@@ -488,10 +488,10 @@ def run_cpt(args):
                                              "eta=0.1"}}))
 
 
-def cdmft_instances(n, n_bath, seed=0):
+def cdmft_instances(n, n_bath, seed=0, n_hyb=None):
     """Seeded CDMFT instances of the batched-CDMFT config: U ~ U[0,12],
     mu ~ U[0,U], bath energies ~ U[-3,3], hybridizations ~ U[0,1] (t = 1,
-    t' = 0)."""
+    t' = 0); n_hyb hybridizations (default one per bath orbital)."""
     import numpy as np
     rng = np.random.default_rng(seed)
     out = []
@@ -499,7 +499,7 @@ def cdmft_instances(n, n_bath, seed=0):
         U = rng.uniform(0, 12)
         mu = rng.uniform(0, U)
         eb = rng.uniform(-3, 3, n_bath)
-        tb = rng.uniform(0, 1, n_bath)
+        tb = rng.uniform(0, 1, n_hyb or n_bath)
         out.append((U, mu, eb, tb))
     return out
 
@@ -507,23 +507,29 @@ def cdmft_instances(n, n_bath, seed=0):
 def run_cdmft(args):
     """CDMFT loops of the plaquette + bath model to convergence, `--concurrency`
     loops in flight at a time on the device (host threads, one loop each):
-    converged points per hour."""
+    converged points per hour.  8 baths: 8 energies + 16 hybridizations (two
+    per bath orbital), the batched-CDMFT configuration; 4 baths: one each."""
     import numpy as np
     import torch
-    from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model, run_many
+    from pyqcm_gb300.cdmft import CDMFT, bath_names, plaquette_bath_model, run_batched, run_many
     torch.cuda.set_device(0)
     nb = args.bath or 8
+    hyb = 2 if nb == 8 else 1
     sector = {4: "R0:N8:S0", 8: "R0:N12:S0"}[nb]
-    names = bath_names(nb)
+    names = bath_names(nb, hyb)
     loops = []
-    for U, mu, eb, tb in cdmft_instances(args.samples or 32, nb, seed=args.seed):
-        lm = plaquette_bath_model(nb, sector)
+    for U, mu, eb, tb in cdmft_instances(args.samples or 32, nb, seed=args.seed, n_hyb=hyb * nb):
+        lm = plaquette_bath_model(nb, sector, hybridizations=hyb)
         params = {"t": 1.0, "tp": 0.0, "U": U, "mu": mu}
         params.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
         lm.set_parameters(params)
-        loops.append(CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64))
+        loops.append(CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=64,
+                           fit=args.fit))
     t_all = time.perf_counter()
-    res = run_many(loops, workers=args.concurrency)
+    if args.batched:
+        res = run_batched(loops, workers=args.concurrency, chunk=args.chunk, groups=args.groups)
+    else:
+        res = run_many(loops, workers=args.concurrency)
     total = time.perf_counter() - t_all
     rows = []
     for c, (x, secs, err) in zip(loops, res):
@@ -538,14 +544,67 @@ def run_cdmft(args):
         "converged": len(conv), "mean_iterations": float(np.mean([r[1] for r in rows])),
         "s_per_point": total / max(len(rows), 1),
         "s_per_iteration": sum(r[2] for r in rows) / max(sum(r[1] for r in rows), 1),
-        "concurrency": args.concurrency,
+        "concurrency": args.concurrency, "bath_fit": args.fit,
+        "driver": f"run_batched (lockstep in {args.groups} group(s): batched ground states and "
+                  "bath fits)" if args.batched
+        else "run_many (independent loops in host threads)",
         "impurity_and_host_s": sum(r[3] for r in rows), "bath_fit_s": sum(r[4] for r in rows),
         "failures": failures, "iteration": "broyden",
         "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"2x2 plaquette + {nb} bath orbitals, sector {sector}, "
-                               f"200 Matsubara frequencies (beta=50), 64x64 k grid, "
-                               f"Broyden CDMFT to the parameters test (1e-4)",
+        "config": {"workload": f"2x2 plaquette + {nb} bath orbitals ({nb} energies, {hyb * nb} "
+                               f"hybridizations), sector {sector}, 200 Matsubara frequencies "
+                               f"(beta=50), 64x64 k grid, Broyden CDMFT to the parameters test (1e-4)",
                    "instances": "seeded U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}))
+
+
+def run_lanczos_batch(args):
+    """Ground states of many uneven impurity sectors: `--samples` seeded
+    instances of the 2x2 plaquette + 4 bath orbitals (U ~ U[0,12],
+    mu ~ U[0,U], eb ~ U[-3,3], tb ~ U[0,1]), each in its sectors N = 7, 8, 9
+    (3,920, 4,900 and 3,920 states), solved by Lanczos to 1e-12: all sectors
+    at once (qcmg_lanczos_batch: each sector's steps replayed from a captured
+    CUDA graph, all sectors side by side) against one sector at a time
+    through the host-driven recurrence (the same FP64 arithmetic); sector
+    solves per second both ways, and the energies must agree bit for bit."""
+    import numpy as np
+    import torch
+    import pyqcm_gb300 as pg
+    from pyqcm_gb300.cdmft import bath_names, plaquette_bath_model
+    torch.cuda.set_device(0)
+    nb = 4
+    names = [n[:-2] for n in bath_names(nb)]
+    hs = []
+    for U, mu, eb, tb in cdmft_instances(args.samples or 256, nb, seed=args.seed):
+        lm = plaquette_bath_model(nb, "R0:N8:S0")
+        lm.finalize()
+        vals = {"t": 1.0, "U": U, "mu": mu}
+        vals.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
+        for sec in ("R0:N7:S1", "R0:N8:S0", "R0:N9:S1"):
+            h = pg.Hamiltonian(lm.cluster, vals, sec)
+            h.set_path(False)
+            hs.append(h)
+    pg.lanczos_batch(hs[:8], tol=1e-12, chunk=args.chunk)  # warm-up (graph machinery, kernels)
+    t0 = time.perf_counter()
+    res = pg.lanczos_batch(hs, tol=1e-12, chunk=args.chunk)
+    t_batch = time.perf_counter() - t0
+    for h in hs[:8]:
+        h.lanczos(tol=1e-12, want_psi=False)
+    t1 = time.perf_counter()
+    single = [h.lanczos(tol=1e-12, want_psi=False)[0] for h in hs]
+    t_single = time.perf_counter() - t1
+    same = all(r[0] == e for r, e in zip(res, single))
+    iters = [r[2] for r in res]
+    print(json.dumps({
+        "metric": "lanczos_batch_sector_solves_per_s", "value": len(hs) / t_batch,
+        "unit": "solves/s", "higher_is_better": True, "sectors": len(hs),
+        "batched_s": t_batch, "one_at_a_time_s": t_single,
+        "one_at_a_time_solves_per_s": len(hs) / t_single, "speedup": t_single / t_batch,
+        "mean_iterations": float(np.mean(iters)), "min_iterations": int(min(iters)),
+        "max_iterations": int(max(iters)), "chunk": args.chunk, "bitwise_equal": same,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"{args.samples or 256} seeded 2x2 plaquette + 4 bath instances x "
+                               "sectors N=7,8,9 (3,920 / 4,900 / 3,920 states), Lanczos to 1e-12",
+                   "instances": "U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}))
 
 
 def run_warmstart(args):
@@ -596,7 +655,8 @@ def main():
     ap.add_argument("--electrons", type=int, default=None,
                     help="electrons in the sector (default: half filling)")
     ap.add_argument("--workload", default="product",
-                    choices=["product", "lanczos", "sef", "cpt", "cdmft", "warmstart"],
+                    choices=["product", "lanczos", "lanczos-batch", "sef", "cpt", "cdmft",
+                             "warmstart"],
                     help="product (the headline line) or one of the secondary measurements")
     ap.add_argument("--bath", type=int, default=None, choices=[4, 8],
                     help="bath orbitals (default: 8 for cdmft, 4 for warmstart, whose "
@@ -605,6 +665,14 @@ def main():
                     help="instances of the CDMFT workload (default 32) or held-out points of "
                          "the warm-start workload (default 3)")
     ap.add_argument("--seed", type=int, default=0, help="seed of the CDMFT instances")
+    ap.add_argument("--chunk", type=int, default=16,
+                    help="lanczos-batch: recurrence steps per captured graph")
+    ap.add_argument("--groups", type=int, default=1,
+                    help="cdmft --batched: lockstep groups driven from their own threads")
+    ap.add_argument("--batched", action="store_true",
+                    help="cdmft: run the loops in lockstep with batched ground states and fits")
+    ap.add_argument("--fit", default="device", choices=["device", "host"],
+                    help="CDMFT bath fit: on the device (qcmg_bath_fit) or SciPy on the host")
     ap.add_argument("--concurrency", type=int, default=8,
                     help="CDMFT loops in flight at a time (one host thread each)")
     ap.add_argument("--reorth", type=int, default=0,
@@ -620,6 +688,8 @@ def main():
         run_reference(args)
     elif args.workload == "lanczos":
         run_lanczos(args)
+    elif args.workload == "lanczos-batch":
+        run_lanczos_batch(args)
     elif args.workload == "sef":
         run_sef(args)
     elif args.workload == "cpt":

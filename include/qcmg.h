@@ -186,6 +186,26 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
                               int max_iter, int reorth, double* E0, double* psi, int* niter,
                               double* alpha, double* beta, int cap);
 
+/* Lanczos ground states of n sectors (handles H[0..n-1], one device, no
+ * handle twice) at once: the three-term recurrence of
+ * qcmg_lanczos_ground_state (no reorthogonalization, FP64 product, seeded
+ * start `seed`) with alpha, beta and the step index kept on the device, each
+ * sector's steps captured once as a CUDA graph of `chunk` steps (rounded up
+ * to even) on a stream of its own and relaunched until the Ritz residual is
+ * below tol (tested after every step, as the reference does) or max_iter
+ * steps; sectors of any sizes run side by side.  Outputs per sector: E0[i],
+ * niter[i] (may be NULL), status[i] (QCMG_OK, QCMG_ERR_NOCONV or
+ * QCMG_ERR_NUMERIC; may be NULL) and, where psi[i] is not NULL (psi itself
+ * may be NULL), the ground-state vector (host array of length dim).  The
+ * energies, coefficients and vectors equal those of
+ * qcmg_lanczos_ground_state on the FP64 path bit for bit.  Replaces the
+ * per-sector LanczosEigenvalue + LanczosEigenvector calls
+ * (src_ed/Hamiltonian/Lanczos.hpp:41-143) that the reference's
+ * low_energy_states makes sector by sector
+ * (src_ed/model_instance.hpp:274-292). */
+int qcmg_lanczos_batch(int n, qcmg_hamiltonian* const* H, unsigned seed, double tol, int max_iter,
+                       int chunk, double* E0, int* niter, double* const* psi, int* status);
+
 /* Breakdown of the last reorthogonalized qcmg_lanczos_ground_state on H:
  * device time of the products and of the Gram-Schmidt sweeps (ms), the
  * sweeps' algorithmic bytes (16 per stored vector element per pass, two
@@ -287,6 +307,22 @@ int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, 
  * lattice_model_instance::set_V combines (src_qcm/CPT.cpp:22-64): R =
  * lattice_model::neighbor, elements = lattice_operator::IGF_elem times the
  * parameter values, Hdiff = H - Hc. */
+/* Cluster self-energy and hybridization function at nz complex frequencies
+ * z (re, im pairs), on the device:
+ *   Gamma(z) = tcb (z - diag(eb))^-1 tcb^dagger,
+ *   Sigma(z) = z - t_c - Gamma(z) - G(z)^-1,
+ * with G(z) from the Q-matrix (e, v as in qcmg_green_function: v
+ * column-major, element (a, i) at a + L i), tcb the L x nb cluster-bath block
+ * (column-major, (r, i) at r + L i), eb the nb bath energies (bath
+ * diagonalized) and t_c the L x L cluster block (row-major complex).
+ * sigma and gamma (may be NULL): nz x L x L complex, row-major [w][r][c].
+ * Replaces model_instance::self_energy and hybridization_function
+ * (src_ed/model_instance.hpp:683-700, 1004-1017), frequency by frequency
+ * there. */
+int qcmg_self_energy(int L, int M, const double* e, const double* v, int nb, const double* tcb,
+                     const double* eb, const double* tc, int nz, const double* z, double* sigma,
+                     double* gamma);
+
 typedef struct qcmg_lattice qcmg_lattice;
 
 int qcmg_lattice_create(int L, int nR, const double* R, int nel, const int32_t* el_r,
@@ -346,6 +382,30 @@ int qcmg_lattice_kmoments(qcmg_lattice* lat, int nz, const double* z, int nkx, i
  * CDMFT_host. */
 int qcmg_cdmft_projected(qcmg_lattice* lat, int nw, const double* w, int kside, int dimk,
                          double* pgf);
+
+/* CDMFT bath fit of n_inst instances at once on the device (one CTA each):
+ * least squares of r_n = sqrt(weights_n) (Gamma(i w_n) + host_n), real and
+ * imaginary parts, Gamma(z) = theta (z - E)^-1 theta^T with theta the
+ * ns x nb cluster-bath block and E = diag(e) the bath energies.  The npar
+ * parameters x enter linearly through nent entries: entry q adds
+ * ent_val[q] * x[ent_par[q]] to theta[ent_i[q]][ent_j[q]] (ent_kind 0) or
+ * to e[ent_j[q]] (ent_kind 1, with ent_i == ent_j), on top of the fixed
+ * parts theta0 (n_inst x ns x nb) and e0 (n_inst x nb).  host: n_inst x nw x
+ * ns x ns complex (re, im), row-major.  x (n_inst x npar): start in, fit
+ * out.  Levenberg-Marquardt on the exact normal equations; stops when the
+ * cost decrease on a well-predicted step is below ftol * cost (status 1),
+ * the step below xtol (xtol + |x|) (2), the gradient below gtol (3), or
+ * after max_iter iterations (0); -1: the damped normal equations stayed
+ * singular.  With ftol = 0 the fit then takes exact Gauss-Newton steps for
+ * as long as they lower the gradient (convergence on the gradient).  cost[k] = 1/2 sum r^2 at the fit.  Limits: ns <= 8, nb <= 16,
+ * npar <= 32, nent <= 128.  Replaces the bath optimization of the
+ * reference's CDMFT step: CDMFT_residuals / CDMFT_distance
+ * (src_qcm/CPT.cpp:519-672) minimized by SciPy from pyqcm/cdmft.py:1539-1640. */
+int qcmg_bath_fit(int n_inst, int ns, int nb, int nw, const double* w, const double* weights,
+                  const double* host, int npar, int nent, const int* ent_par, const int* ent_kind,
+                  const int* ent_i, const int* ent_j, const double* ent_val, const double* theta0,
+                  const double* e0, double* x, int max_iter, double xtol, double ftol,
+                  double gtol, double* cost, int* iters, int* status);
 
 /* ---------------------------------------------------------------------------
  * Multilayer perceptron of the learned CDMFT warm start (no counterpart in

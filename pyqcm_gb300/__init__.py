@@ -6,9 +6,9 @@ this package is the host-side mirror of pyqcm's interface for that path.
 """
 from ._lib import QcmgError, lib  # noqa: F401
 from .ed import (GLOBAL, ClusterModel, Hamiltonian, ModelInstance, Sector,  # noqa: F401
-                 apply_c, green_function, halfbasis, halfbasis_rank, set_global_parameter,
-                 streamline)
+                 apply_c, green_function, halfbasis, halfbasis_rank, lanczos_batch,
+                 set_global_parameter, streamline)
 
 __all__ = ["QcmgError", "lib", "GLOBAL", "ClusterModel", "Hamiltonian", "ModelInstance",
-           "Sector", "apply_c", "green_function", "halfbasis", "halfbasis_rank",
+           "Sector", "apply_c", "green_function", "halfbasis", "halfbasis_rank", "lanczos_batch",
            "set_global_parameter", "streamline"]

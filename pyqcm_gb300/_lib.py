@@ -57,6 +57,7 @@ SIGNATURES = {
     "qcmg_seeded_vector": (c_int, [c_size_t, c_uint, vp]),
     "qcmg_lanczos_ground_state": (c_int, [vp, vp, c_uint, c_double, c_int, c_int, dbl_p, vp,
                                           int_p, vp, vp, c_int]),
+    "qcmg_lanczos_batch": (c_int, [c_int, vp, c_uint, c_double, c_int, c_int, vp, vp, vp, vp]),
     "qcmg_lanczos_last_stats": (c_int, [vp, dbl_p, dbl_p, dbl_p, int_p, int_p, int_p]),
     "qcmg_band_lanczos": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p, vp,
                                   vp, c_int]),
@@ -69,6 +70,7 @@ SIGNATURES = {
                                    int_p, vp, vp, vp, c_int]),
     "qcmg_apply_c": (c_int, [c_int, c_int, c_int, c_int, c_int, vp, vp, c_double, c_uint]),
     "qcmg_green_function": (c_int, [c_int, c_int, vp, vp, c_int, vp, vp]),
+    "qcmg_self_energy": (c_int, [c_int, c_int, vp, vp, c_int, vp, vp, vp, c_int, vp, vp, vp]),
     "qcmg_lattice_create": (c_int, [c_int, c_int, vp, c_int, vp, vp, vp, vp, vp, vp,
                                     ctypes.POINTER(vp)]),
     "qcmg_lattice_destroy": (c_int, [vp]),
@@ -78,6 +80,8 @@ SIGNATURES = {
     "qcmg_cdmft_projected": (c_int, [vp, c_int, vp, c_int, c_int, vp]),
     "qcmg_lattice_kmean": (c_int, [vp, c_int, vp, c_int, c_int, c_int, c_double, vp]),
     "qcmg_lattice_kmoments": (c_int, [vp, c_int, vp, c_int, c_int, c_int, c_double, c_int, vp, vp]),
+    "qcmg_bath_fit": (c_int, [c_int, c_int, c_int, c_int, vp, vp, vp, c_int, c_int, vp, vp, vp, vp,
+                              vp, vp, vp, vp, c_int, c_double, c_double, c_double, vp, vp, vp]),
     "qcmg_mlp_create": (c_int, [c_int, vp, ctypes.POINTER(vp)]),
     "qcmg_mlp_destroy": (c_int, [vp]),
     "qcmg_mlp_num_params": (c_int, [vp, size_p]),

@@ -11,8 +11,10 @@ Restates the reference's CDMFT procedure (pyqcm/cdmft.py):
   hybridization function matches -G_host;
 - the bath fit by least squares on the residuals
   r_n = sqrt(w_n) (Gamma(iw_n) + G_host(iw_n)), real and imaginary parts
-  (CDMFT_residuals, src_qcm/CPT.cpp:556-610), with scipy's 'trf' solver and
-  the reference's tolerances (optimize(method='trf'), cdmft.py:1539-1640);
+  (CDMFT_residuals, src_qcm/CPT.cpp:556-610), with the reference's
+  tolerances (optimize(method='trf'), cdmft.py:1539-1640): on the device
+  (qcmg_bath_fit, Levenberg-Marquardt on the exact normal equations) for a
+  diagonal bath, else with scipy's 'trf' solver;
 - the outer fixed-point iteration with damping (fixed_point_iteration,
   pyqcm/__init__.py:2773-2845).
 
@@ -88,6 +90,12 @@ class BathFit:
         self.sw = np.sqrt(np.asarray(weights, np.float64))
         self.host = np.asarray(host, np.complex128)
         self.nb = self.E0.shape[0]
+
+    def diagonal_bath(self):
+        """True when the bath has no bath-bath hopping (E diagonal for every
+        parameter value): the form the device fit takes."""
+        off = lambda m: np.count_nonzero(m - np.diag(np.diag(m)))
+        return not off(self.E0) and not any(off(d) for d in self.dE)
 
     def blocks(self, x):
         th = self.theta0.copy()
@@ -172,6 +180,41 @@ def fit_bath(fit, x0, accur_bath=1e-6, accur_dist=1e-8, max_nfev=2000):
     return sol.x, sol.nfev
 
 
+def fit_bath_device(fits, x0s, accur_bath=1e-6, accur_dist=1e-8, gtol=1e-12, max_iter=200):
+    """The bath fits of several instances at once on the device
+    (qcmg_bath_fit: one CTA per instance runs Levenberg-Marquardt on the
+    exact normal equations).  fits: BathFit objects sharing one parameter
+    structure and frequency grid; x0s: their start vectors.  Returns
+    (x (n, npar), cost (n,), iterations (n,), status (n,))."""
+    from ._lib import check, lib, ptr
+    f0 = fits[0]
+    n = len(fits)
+    P, A, B, V = f0.nz_theta
+    PE, BE, CE, VE = f0.nz_E
+    if not all(f.diagonal_bath() for f in fits):
+        raise ValueError("the device bath fit takes a diagonal bath (bath energies only)")
+    ent_par = np.ascontiguousarray(np.concatenate([P, PE]).astype(np.int32))
+    ent_kind = np.ascontiguousarray(np.concatenate([np.zeros(len(P)), np.ones(len(PE))]).astype(np.int32))
+    ent_i = np.ascontiguousarray(np.concatenate([A, BE]).astype(np.int32))
+    ent_j = np.ascontiguousarray(np.concatenate([B, CE]).astype(np.int32))
+    ent_v = np.ascontiguousarray(np.concatenate([V, VE]).astype(np.float64))
+    w = np.ascontiguousarray(f0.iw.imag)
+    wt = np.ascontiguousarray(f0.sw ** 2)
+    host = np.ascontiguousarray(np.stack([f.host for f in fits]).astype(np.complex128))
+    th0 = np.ascontiguousarray(np.stack([f.theta0 for f in fits]).astype(np.float64))
+    e0 = np.ascontiguousarray(np.stack([np.diag(f.E0) for f in fits]).astype(np.float64))
+    x = np.ascontiguousarray(np.array(x0s, np.float64).reshape(n, -1))
+    npar = x.shape[1]
+    cost = np.zeros(n)
+    it = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    check(lib().qcmg_bath_fit(n, f0.ns, f0.nb, len(w), ptr(w), ptr(wt), ptr(host), npar,
+                              len(ent_par), ptr(ent_par), ptr(ent_kind), ptr(ent_i), ptr(ent_j),
+                              ptr(ent_v), ptr(th0), ptr(e0), ptr(x), max_iter, accur_bath,
+                              accur_dist, gtol, ptr(cost), ptr(it), ptr(st)))
+    return x, cost, it, st
+
+
 class CDMFT:
     """The CDMFT loop on a lattice model (pyqcm.cdmft.CDMFT with
     iteration='fixed_point', convergence='parameters', method='trf').
@@ -182,9 +225,12 @@ class CDMFT:
 
     def __init__(self, model, varia, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=32,
                  miniter=0, depth=2, accur=1e-4, accur_bath=1e-6, accur_dist=1e-8, damping=0.0,
-                 max_nfev=2000, x0=None, iteration="broyden", verbose=False):
+                 max_nfev=2000, x0=None, iteration="broyden", verbose=False, fit="device"):
         if iteration not in ("broyden", "fixed_point"):
             raise ValueError("iteration must be 'broyden' or 'fixed_point'")
+        if fit not in ("device", "host"):
+            raise ValueError("fit must be 'device' (qcmg_bath_fit) or 'host' (SciPy)")
+        self.fit = fit
         self.iteration = iteration
         self.model = model
         self.varia = list(varia)
@@ -204,52 +250,94 @@ class CDMFT:
         self.history = []
         self.time_ed = self.time_fit = 0.0
 
-    def step(self, x):
-        """One CDMFT step from bath x: returns the fitted bath."""
+    # -- one CDMFT step, in phases (run_batched runs each phase for many loops)
+    def _prepare(self, x):
+        """Sets the bath x on the model and makes the instance; returns the
+        Hamiltonians of its impurity ground-state sectors."""
         params = dict(self.model.params)
         params.update({v: float(xv) for v, xv in zip(self.varia, x)})
         self.model.set_parameters(params)
-        t0 = time.perf_counter()
-        inst = self.model.instance()
+        self._t0 = time.perf_counter()
+        self._inst = self.model.instance()
+        return self._inst.cluster.gs_hamiltonians()
+
+    def _host_fits(self, solved=None):
+        """Impurity ground state (from `solved` when given), Green function and
+        host function; returns one BathFit per spin block."""
+        inst = self._inst
+        inst.cluster.ground_state(solved)
         host = inst.CDMFT_host(self.wr, self.cw, kside=self.kside)
-        t1 = time.perf_counter()
+        self._t1 = time.perf_counter()
         values = dict(inst.cluster.values)
-        newx = np.array(x, np.float64)
-        dist = 0.0
-        normal = not (inst.cluster.mixing & 4)
-        for sd, H in host.items():
-            fit = BathFit(self.model.cluster, values, self.cnames, self.wr, self.cw, H, sd)
-            newx, _ = fit_bath(fit, newx, self.accur_bath, self.accur_dist, self.max_nfev)
-            dist += fit.distance(newx, normal)
+        return [BathFit(self.model.cluster, values, self.cnames, self.wr, self.cw, H, sd)
+                for sd, H in host.items()]
+
+    def _fit_one(self, fit, x):
+        if self.fit == "device" and fit.diagonal_bath():
+            xs, _, _, _ = fit_bath_device([fit], [x], self.accur_bath, self.accur_dist,
+                                          max_iter=max(1, self.max_nfev // 10))
+            return xs[0]
+        return fit_bath(fit, x, self.accur_bath, self.accur_dist, self.max_nfev)[0]
+
+    def _finish(self, fits, newx):
+        normal = not (self._inst.cluster.mixing & 4)
+        self.dist = sum(f.distance(newx, normal) for f in fits)
         t2 = time.perf_counter()
-        self.time_ed += t1 - t0
-        self.time_fit += t2 - t1
-        self.dist = dist
-        self.E0 = inst.cluster.E0
+        self.time_ed += self._t1 - self._t0
+        self.time_fit += t2 - self._t1
+        self.E0 = self._inst.cluster.E0
         return newx
+
+    def step(self, x):
+        """One CDMFT step from bath x: returns the fitted bath (the spin
+        blocks' fits in turn, each starting from the previous one's bath)."""
+        self._prepare(x)
+        fits = self._host_fits()
+        newx = np.array(x, np.float64)
+        for fit in fits:
+            newx = self._fit_one(fit, newx)
+        return self._finish(fits, newx)
 
     def run(self):
         """Iterates to self-consistency (Broyden or fixed point, as the
         reference's CDMFT does) until the fitted bath passes the parameters
         test; returns the converged bath."""
-        if self.iteration == "broyden":
-            self._broyden()
-        else:
-            self._fixed_point()
+        gen = self._iterate()
+        x = next(gen)
+        try:
+            while True:
+                x = gen.send(self.step(x))
+        except StopIteration:
+            pass
+        return self._settle()
+
+    def _settle(self):
         params = dict(self.model.params)
         params.update({v: float(xv) for v, xv in zip(self.varia, self.x)})
         self.model.set_parameters(params)
         return self.x
+
+    def _iterate(self):
+        """The outer iteration as a generator: yields the bath at which a CDMFT
+        step is needed and receives the step's fitted bath."""
+        if self.iteration == "broyden":
+            yield from self._broyden()
+        else:
+            yield from self._fixed_point()
+
+    def _record(self, xs):
+        self.xs = xs
+        self.history.append(xs.copy())
 
     def _fixed_point(self):
         """x <- step(x), damped (fixed_point_iteration, pyqcm/__init__.py:2773-2845)."""
         x0 = self.x.copy()
         it = 0
         while True:
-            xs = self.step(x0)
+            xs = yield x0
+            self._record(xs)
             x = xs + self.damping * (x0 - xs)   # (alpha - 1) F(x0) + x0, F = x0 - step(x0)
             it += 1
-            self.history.append(xs.copy())
             if self.verbose:
                 print(f"CDMFT iteration {it}: |dx| = {np.linalg.norm(x - x0):.3g}, "
                       f"distance = {self.dist:.3g}")
@@ -268,9 +356,10 @@ class CDMFT:
         fitted bath of each step."""
         n = len(self.x)
         I = (1.0 + self.damping) * np.eye(n)
-        F = lambda x: x - self._step_record(x)
         x = self.x.copy()
-        f0 = F(x)
+        xs = yield x
+        self._record(xs)
+        f0 = x - xs
         f = f0.copy()
         it = 0
         while True:
@@ -286,7 +375,9 @@ class CDMFT:
                 break
             if self.conv.test(self.xs) and it >= self.miniter:
                 break
-            f = F(x)
+            xs = yield x
+            self._record(xs)
+            f = x - xs
             df = f - f0
             f0 = f.copy()
             I += np.outer(dx - I @ df, dx) @ I / (dx @ (I @ df))
@@ -296,10 +387,138 @@ class CDMFT:
         self.x = x
         self.niter = it + 1
 
-    def _step_record(self, x):
-        self.xs = self.step(x)
-        self.history.append(self.xs.copy())
-        return self.xs
+
+def run_batched(loops, workers=8, chunk=16, groups=1):
+    """Runs CDMFT loops in lockstep with their device work batched (see
+    _lockstep).  groups > 1 splits the loops round-robin into that many
+    lockstep groups driven from host threads of their own, so that one group's
+    batched ground states run on the device while another group's Green
+    functions, host functions and fits run (workers are shared out among the
+    groups).  Returns [(x, seconds, error)] in the order of `loops`."""
+    groups = max(1, min(groups, len(loops)))
+    if groups == 1:
+        return _lockstep(loops, workers, chunk)
+    from concurrent.futures import ThreadPoolExecutor
+    idx = [list(range(g, len(loops), groups)) for g in range(groups)]
+    per = max(1, workers // groups)
+    with ThreadPoolExecutor(max_workers=groups) as ex:
+        futs = [ex.submit(_lockstep, [loops[i] for i in ix], per, chunk) for ix in idx]
+        res = [f.result() for f in futs]
+    out = [None] * len(loops)
+    for ix, r in zip(idx, res):
+        for i, v in zip(ix, r):
+            out[i] = v
+    return out
+
+
+def _lockstep(loops, workers=8, chunk=16):
+    """Runs CDMFT loops in lockstep, one step of every unfinished loop at a
+    time, with the device work of each step batched across the loops:
+      1. every loop's impurity ground states in one lanczos_batch call (each
+         sector's Lanczos steps replayed from a captured CUDA graph, all
+         sectors side by side);
+      2. the Green and host functions of each loop, in host threads (their
+         device work overlaps);
+      3. every loop's bath fit in one qcmg_bath_fit launch (one CTA per loop),
+         per spin block, when the loops share one bath structure and use the
+         device fit (each loop's own fit otherwise);
+      4. each loop's Broyden or fixed-point update.
+    The loops' iterates are those of running them one by one (the ground
+    states are bitwise the same on the FP64 path).  Returns [(x, seconds,
+    error)] in the order of `loops`, like run_many."""
+    from concurrent.futures import ThreadPoolExecutor
+    from .ed import lanczos_batch
+    t_start = time.perf_counter()
+    n = len(loops)
+    out = [None] * n
+    gens, pending = {}, {}
+
+    def fail(i, e):
+        out[i] = (None, time.perf_counter() - t_start, e)
+        pending.pop(i, None)
+
+    for i, c in enumerate(loops):
+        try:
+            gens[i] = c._iterate()
+            pending[i] = next(gens[i])
+        except Exception as e:  # noqa: BLE001 - reported per loop
+            fail(i, e)
+    with ThreadPoolExecutor(max_workers=max(1, workers)) as ex:
+        while pending:
+            # 1. instances and their ground-state sectors, solved together
+            hs = {}
+            for i in list(pending):
+                try:
+                    hs[i] = loops[i]._prepare(pending[i])
+                except Exception as e:  # noqa: BLE001
+                    fail(i, e)
+            allh = [h for i in pending for h in hs[i]]
+            res = lanczos_batch(allh, want_psi=True, chunk=chunk, raise_errors=False)
+            solved, k = {}, 0
+            for i in list(pending):
+                solved[i] = {}
+                for h in hs[i]:
+                    e0, psi, _, err = res[k]
+                    k += 1
+                    if err is not None and i in pending:
+                        fail(i, err)
+                    solved[i][h] = (e0, psi)
+            # 2. Green and host functions per loop
+            live = list(pending)
+            futs = {i: ex.submit(loops[i]._host_fits, solved[i]) for i in live}
+            fits = {}
+            for i in live:
+                try:
+                    fits[i] = futs[i].result()
+                except Exception as e:  # noqa: BLE001
+                    fail(i, e)
+            # 3. bath fits: one device launch per spin block for the loops
+            #    that share the first loop's structure, the others one by one
+            live = list(pending)
+            newx = {i: np.array(pending[i], np.float64) for i in live}
+            nblk = max((len(fits[i]) for i in live), default=0)
+            for blk in range(nblk):
+                dev = [i for i in live if loops[i].fit == "device" and len(fits[i]) > blk
+                       and fits[i][blk].diagonal_bath()]
+                if dev:
+                    ref = fits[dev[0]][blk]
+                    same = [i for i in dev if _same_structure(fits[i][blk], ref)]
+                    c0 = loops[same[0]]
+                    xs, _, _, _ = fit_bath_device([fits[i][blk] for i in same],
+                                                  [newx[i] for i in same], c0.accur_bath,
+                                                  c0.accur_dist,
+                                                  max_iter=max(1, c0.max_nfev // 10))
+                    for j, i in enumerate(same):
+                        newx[i] = xs[j]
+                    dev = [i for i in dev if i not in same]
+                for i in live:
+                    if len(fits[i]) > blk and (i in dev or loops[i].fit != "device"
+                                               or not fits[i][blk].diagonal_bath()):
+                        try:
+                            newx[i] = loops[i]._fit_one(fits[i][blk], newx[i])
+                        except Exception as e:  # noqa: BLE001
+                            fail(i, e)
+            # 4. the outer iterations
+            for i in list(pending):
+                c = loops[i]
+                try:
+                    xs = c._finish(fits[i], newx[i])
+                    pending[i] = gens[i].send(xs)
+                except StopIteration:
+                    out[i] = (c._settle(), time.perf_counter() - t_start, None)
+                    pending.pop(i)
+                except Exception as e:  # noqa: BLE001
+                    fail(i, e)
+    return out
+
+
+def _same_structure(a, b):
+    """True when two BathFits share parameters, entries and frequency grid
+    (one qcmg_bath_fit launch can take both)."""
+    return (len(a.names) == len(b.names) and a.ns == b.ns and a.nb == b.nb
+            and np.array_equal(a.iw, b.iw) and np.array_equal(a.sw, b.sw)
+            and all(np.array_equal(x, y) for x, y in zip(a.nz_theta, b.nz_theta))
+            and all(np.array_equal(x, y) for x, y in zip(a.nz_E, b.nz_E)))
 
 
 def run_many(loops, workers=4):

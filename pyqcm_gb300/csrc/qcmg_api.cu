@@ -626,6 +626,35 @@ int qcmg_green_function(int L, int M, const double* e, const double* v, int nz, 
   });
 }
 
+int qcmg_self_energy(int L, int M, const double* e, const double* v, int nb, const double* tcb,
+                     const double* eb, const double* tc, int nz, const double* z, double* sigma,
+                     double* gamma) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(L > 0 && L <= 32 && M >= 0 && nb >= 0 && nz >= 0, "invalid sizes");
+    QCMG_CHECK_ARG(tc && z && sigma && (M == 0 || (e && v)) && (nb == 0 || (tcb && eb)),
+                   "NULL argument");
+    if (nz == 0) return;
+    use_device();
+    DevBuf<double> de, dv, dtcb, deb, dtc, dz, ds, dg;
+    if (M) {
+      de.upload(e, M, 0);
+      dv.upload(v, (size_t)2 * L * M, 0);
+    }
+    if (nb) {
+      dtcb.upload(tcb, (size_t)2 * L * nb, 0);
+      deb.upload(eb, nb, 0);
+    }
+    dtc.upload(tc, (size_t)2 * L * L, 0);
+    dz.upload(z, (size_t)2 * nz, 0);
+    ds.alloc((size_t)2 * L * L * nz);
+    if (gamma) dg.alloc((size_t)2 * L * L * nz);
+    self_energy_batch(L, M, de.p, dv.p, nb, dtcb.p, deb.p, dtc.p, nz, dz.p, ds.p,
+                      gamma ? dg.p : nullptr, 0);
+    QCMG_CUDA(cudaMemcpy(sigma, ds.p, (size_t)2 * L * L * nz * 8, cudaMemcpyDeviceToHost));
+    if (gamma) QCMG_CUDA(cudaMemcpy(gamma, dg.p, (size_t)2 * L * L * nz * 8, cudaMemcpyDeviceToHost));
+  });
+}
+
 int qcmg_lattice_create(int L, int nR, const double* R, int nel, const int32_t* el_r,
                         const int32_t* el_c, const int32_t* el_n, const double* el_v,
                         const double* hdiff, const double* gpos, qcmg_lattice** out) {

@@ -109,6 +109,85 @@ __global__ void k_replay(double* __restrict__ r, double* __restrict__ q, double*
   }
 }
 
+// Device-scalar forms of the Lanczos recurrence for captured step sequences:
+// the step index *jp and the coefficients alpha[], beta[] live in device
+// memory, and a set *done turns each kernel into a no-op.  Same arithmetic,
+// grids and summation order as scale2 / Reducer::dot / Reducer::axpy_norm2,
+// so a captured run reproduces the host-driven one bit for bit.
+__global__ void k_lzb_scale2(double* __restrict__ r, double* __restrict__ q, size_t n,
+                             const double* __restrict__ beta, const int* __restrict__ jp,
+                             const int* __restrict__ done) {
+  if (*done) return;
+  const int j = *jp;
+  if (j == 0) return;
+  const double b = beta[j - 1], s1 = 1.0 / b, s2 = -b;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    r[i] *= s1;
+    q[i] *= s2;
+  }
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_lzb_dot_partial(const double* __restrict__ x,
+                                                                 const double* __restrict__ y,
+                                                                 size_t n, double* __restrict__ part,
+                                                                 const int* __restrict__ done) {
+  if (*done) return;
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    s = fma(x[i], y[i], s);
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+__global__ void __launch_bounds__(kRedBlocks) k_lzb_alpha(const double* __restrict__ part, int np,
+                                                          double* __restrict__ alpha,
+                                                          const int* __restrict__ jp,
+                                                          const int* __restrict__ done) {
+  if (*done) return;
+  double s = (threadIdx.x < np) ? part[threadIdx.x] : 0.0;
+  s = block_sum(s);
+  if (threadIdx.x == 0) alpha[*jp] = s;
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_lzb_axpy_norm(double* __restrict__ r,
+                                                               const double* __restrict__ q,
+                                                               size_t n,
+                                                               const double* __restrict__ alpha,
+                                                               const int* __restrict__ jp,
+                                                               double* __restrict__ part,
+                                                               const int* __restrict__ done) {
+  if (*done) return;
+  const double a = alpha[*jp];
+  double s = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x) {
+    double v = fma(-a, q[i], r[i]);
+    r[i] = v;
+    s = fma(v, v, s);
+  }
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[blockIdx.x] = s;
+}
+
+// beta[j] = sqrt(sum of the partials), then j <- j + 1; the run stops
+// itself (done = 2) when j reaches the coefficient arrays' capacity.
+__global__ void __launch_bounds__(kRedBlocks) k_lzb_beta(const double* __restrict__ part, int np,
+                                                         double* __restrict__ beta,
+                                                         int* __restrict__ jp, int* __restrict__ done,
+                                                         int cap) {
+  if (*done) return;
+  double s = (threadIdx.x < np) ? part[threadIdx.x] : 0.0;
+  s = block_sum(s);
+  if (threadIdx.x == 0) {
+    const int j = *jp;
+    beta[j] = sqrt(s);
+    *jp = j + 1;
+    if (j + 1 >= cap) *done = 2;
+  }
+}
+
 static unsigned ew_grid(size_t n) {
   size_t g = (n + 255) / 256;
   if (g < 1) g = 1;
@@ -186,6 +265,23 @@ void scale(double* x, double a, size_t n, cudaStream_t s) {
   if (!n) return;
   k_scale<<<ew_grid(n), 256, 0, s>>>(x, a, n);
   QCMG_CUDA(cudaGetLastError());
+}
+
+void lanczos_step_nodes(const LanczosDevState& st, double* r, double* q, size_t n, GraphChain& gc,
+                        const std::function<void(const double*, double*)>& product) {
+  const unsigned g = red_grid(n);
+  gc.add(k_lzb_scale2, dim3(ew_grid(n)), dim3(256), 0, r, q, n, (const double*)st.beta,
+         (const int*)st.j, (const int*)st.done);
+  product(r, q);  // q += H r, a node of the same chain
+  // the roles swap: q is the new residual, r the current basis vector
+  gc.add(k_lzb_dot_partial, dim3(g), dim3(kRedThreads), 0, (const double*)r, (const double*)q, n,
+         st.part, (const int*)st.done);
+  gc.add(k_lzb_alpha, dim3(1), dim3(kRedBlocks), 0, (const double*)st.part, (int)g, st.alpha,
+         (const int*)st.j, (const int*)st.done);
+  gc.add(k_lzb_axpy_norm, dim3(g), dim3(kRedThreads), 0, q, (const double*)r, n,
+         (const double*)st.alpha, (const int*)st.j, st.part, (const int*)st.done);
+  gc.add(k_lzb_beta, dim3(1), dim3(kRedBlocks), 0, (const double*)st.part, (int)g, st.beta, st.j,
+         st.done, st.cap);
 }
 
 void replay_step(double* r, double* q, double* gs, double alpha, double beta, double c, size_t n,

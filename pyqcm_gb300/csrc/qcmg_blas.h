@@ -1,6 +1,8 @@
 // Vector kernels of the Krylov solvers (host launch wrappers).
 #pragma once
 
+#include <functional>
+
 #include "qcmg_internal.h"
 
 namespace qcmg {
@@ -33,5 +35,24 @@ void scale2(double* r, double s1, double* q, double s2, size_t n, cudaStream_t s
 void scale(double* x, double a, size_t n, cudaStream_t s);
 void replay_step(double* r, double* q, double* gs, double alpha, double beta, double c, size_t n,
                  cudaStream_t s);
+
+// Device state of a Lanczos recurrence whose step index and coefficients
+// stay on the device (for step sequences captured in a CUDA graph).
+struct LanczosDevState {
+  double* alpha;  // cap
+  double* beta;   // cap
+  double* part;   // kRedBlocks partial sums
+  int* j;         // steps done
+  int* done;      // nonzero: every step kernel returns at once
+  int cap;
+};
+
+// One recurrence step of LanczosEigenvalue on (r, q) with the scalars on
+// the device, appended to a graph chain: r /= beta[j-1], q *= -beta[j-1]
+// (j > 0); q += H r (product, which appends its own node); alpha[j] =
+// <r, q>; q -= alpha[j] r; beta[j] = |q|; j += 1.  The next step takes
+// (q, r): the two buffers swap roles every step.
+void lanczos_step_nodes(const LanczosDevState& st, double* r, double* q, size_t n, GraphChain& gc,
+                        const std::function<void(const double*, double*)>& product);
 
 }  // namespace qcmg

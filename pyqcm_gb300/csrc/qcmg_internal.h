@@ -1,6 +1,9 @@
 // Internal declarations of the qcmg engine (not part of the C ABI).
 #pragma once
 
+#include <tuple>
+#include <utility>
+
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -178,4 +181,37 @@ struct qcmg_hamiltonian {
 namespace qcmg {
 // Matrix-free factorized product y (+)= H x on the handle's stream.
 void matvec(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
+// A chain of kernel nodes added to a CUDA graph explicitly (no stream
+// capture, so no other host thread's device-wide synchronization can
+// invalidate it): each node depends on the previous one.
+struct GraphChain {
+  cudaGraph_t graph = nullptr;
+  cudaGraphNode_t last = nullptr;
+  template <class... KArgs, class... Args>
+  void add(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, Args... args) {
+    static_assert(sizeof...(KArgs) == sizeof...(Args), "argument count");
+    add_impl(kern, grid, block, smem, std::index_sequence_for<KArgs...>{},
+             std::tuple<KArgs...>(args...));
+  }
+
+ private:
+  template <class... KArgs, size_t... I>
+  void add_impl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem,
+                std::index_sequence<I...>, std::tuple<KArgs...> vals) {
+    void* ptrs[sizeof...(KArgs) > 0 ? sizeof...(KArgs) : 1] = {(void*)&std::get<I>(vals)...};
+    cudaKernelNodeParams p = {};
+    p.func = (void*)kern;
+    p.gridDim = grid;
+    p.blockDim = block;
+    p.sharedMemBytes = (unsigned)smem;
+    p.kernelParams = ptrs;
+    p.extra = nullptr;
+    cudaGraphNode_t node;
+    QCMG_CUDA(cudaGraphAddKernelNode(&node, graph, last ? &last : nullptr, last ? 1 : 0, &p));
+    last = node;
+  }
+};
+
+// The FP64 product y (+)= H x as one kernel node of a graph chain.
+void matvec_node(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate, GraphChain& gc);
 }  // namespace qcmg

@@ -131,6 +131,68 @@ __global__ void k_freq_prep(int L, int nw, const double2* __restrict__ G,  // nw
   if (threadIdx.x == 0) logdetG[w] = ldet;  // the pivots are those of G itself
 }
 
+// Sigma(z) = z - base with base = G^-1 + Gamma + t_c (k_freq_prep with the
+// constant block -t_c); Gamma(z) alone for the hybridization function.
+__global__ void k_sigma_from_base(int L, int nw, const double2* __restrict__ z,
+                                  double2* __restrict__ base) {
+  const int w = blockIdx.x;
+  double2* B = base + (size_t)w * L * L;
+  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+    const int r = idx / L, c = idx % L;
+    const double2 b = B[idx];
+    B[idx] = make_double2((r == c ? z[w].x : 0.0) - b.x, (r == c ? z[w].y : 0.0) - b.y);
+  }
+}
+
+__global__ void k_gamma(int L, int nw, const double2* __restrict__ z, int nb,
+                        const double2* __restrict__ tcb, const double* __restrict__ eb,
+                        double2* __restrict__ out) {
+  const int w = blockIdx.x;
+  const double2 zw = z[w];
+  for (int idx = threadIdx.x; idx < L * L; idx += blockDim.x) {
+    const int r = idx / L, c = idx % L;
+    double gx = 0.0, gy = 0.0;
+    for (int i = 0; i < nb; ++i) {  // the same sum as in k_freq_prep
+      double2 a = tcb[r + (size_t)L * i], b = tcb[c + (size_t)L * i];
+      double re = zw.x - eb[i], im = zw.y, den = re * re + im * im;
+      double ur = re / den, ui = -im / den;
+      double pr = a.x * b.x + a.y * b.y, pi = a.y * b.x - a.x * b.y;
+      gx += pr * ur - pi * ui;
+      gy += pr * ui + pi * ur;
+    }
+    out[(size_t)w * L * L + idx] = make_double2(gx, gy);
+  }
+}
+
+void self_energy_batch(int L, int M, const double* e, const double* v, int nb, const double* tcb,
+                       const double* eb, const double* tc, int nz, const double* z, double* sigma,
+                       double* gamma, cudaStream_t s) {
+  QCMG_CHECK_ARG(L > 0 && L <= 32, "Green function dimension must be 1..32");
+  DevBuf<double> G, ldg, mtc;
+  G.alloc((size_t)2 * L * L * nz);
+  if (M > 0)
+    green_function_batch(L, M, e, v, nz, z, G.p, s);
+  else
+    QCMG_CUDA(cudaMemsetAsync(G.p, 0, G.n * 8, s));
+  // constant block -t_c
+  std::vector<double> h((size_t)2 * L * L);
+  QCMG_CUDA(cudaMemcpyAsync(h.data(), tc, h.size() * 8, cudaMemcpyDeviceToHost, s));
+  QCMG_CUDA(cudaStreamSynchronize(s));
+  for (double& x : h) x = -x;
+  mtc.upload(h.data(), h.size(), s);
+  ldg.alloc(nz);
+  const size_t smem = (size_t)L * 2 * L * sizeof(double2);
+  k_freq_prep<<<nz, 128, smem, s>>>(L, nz, (const double2*)G.p, (const double2*)z, nb,
+                                    (const double2*)tcb, eb, (const double2*)mtc.p,
+                                    (double2*)sigma, ldg.p);
+  k_sigma_from_base<<<nz, 128, 0, s>>>(L, nz, (const double2*)z, (double2*)sigma);
+  if (gamma)
+    k_gamma<<<nz, 128, 0, s>>>(L, nz, (const double2*)z, nb, (const double2*)tcb, eb,
+                               (double2*)gamma);
+  QCMG_CUDA(cudaGetLastError());
+  QCMG_CUDA(cudaStreamSynchronize(s));  // mtc, G go out of scope
+}
+
 // ---------------------------------------------------------------------------
 // Per-point kernel.  MODE 0: SEF (sum of log|det M| weighted), MODE 1: CPT
 // periodized g(K,z), MODE 2: mean of M^-1 (CDMFT projected GF).

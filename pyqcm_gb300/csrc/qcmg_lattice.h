@@ -53,6 +53,15 @@ struct Lattice {
                 const double* R, double* out, cudaStream_t s);
 };
 
+// Cluster self-energy Sigma(z) = z - t_c - Gamma(z) - G(z)^-1 for nz complex
+// frequencies, with G(z) from the Q-matrix (L x M, column-major a + L i) and
+// Gamma(z) from the cluster-bath block tcb (column-major r + L i) and the
+// bath energies eb; t_c row-major; all arrays on the device; sigma (and
+// gamma when not null) nz x L x L row-major.
+void self_energy_batch(int L, int M, const double* e, const double* v, int nb, const double* tcb,
+                       const double* eb, const double* tc, int nz, const double* z, double* sigma,
+                       double* gamma, cudaStream_t s);
+
 }  // namespace qcmg
 
 struct qcmg_lattice {

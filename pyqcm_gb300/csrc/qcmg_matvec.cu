@@ -90,6 +90,38 @@ static void launch_inter(qcmg_hamiltonian* H, const double* x, double* y, bool a
   QCMG_CUDA(cudaGetLastError());
 }
 
+template <int INTER>
+static void node_inter(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate,
+                       GraphChain& gc) {
+  const size_t smem = (size_t)H->du * sizeof(double);
+  const int threads = H->du >= 512 ? 512 : (H->du >= 256 ? 256 : 128);
+  int sms = 0;
+  QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, H->device));
+  unsigned grid = (unsigned)std::min<size_t>(H->dd, (size_t)sms * 8);
+  if (grid < 1) grid = 1;
+  int max_optin = 0;
+  QCMG_CUDA(cudaDeviceGetAttribute(&max_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, H->device));
+  auto& up = H->up;
+  auto& dn = H->dn;
+  const bool in_smem = smem <= (size_t)max_optin;
+  auto kern = in_smem ? k_matvec_f64<INTER, true> : k_matvec_f64<INTER, false>;
+  if (in_smem && smem > 48 * 1024)
+    QCMG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  gc.add(kern, dim3(grid), dim3(threads), in_smem ? smem : 0, H->du, H->dd, H->L,
+         (const uint32_t*)up.rowptr.p, (const uint32_t*)up.col.p, (const double*)up.val.p,
+         (const double*)up.diag.p, (const uint32_t*)dn.rowptr.p, (const uint32_t*)dn.col.p,
+         (const double*)dn.val.p, (const double*)dn.diag.p, (const uint32_t*)up.bin.p,
+         (const uint32_t*)dn.bin.p, H->U, (const double*)H->wdn.p, x, y, accumulate ? 1 : 0);
+}
+
+void matvec_node(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate, GraphChain& gc) {
+  switch (H->inter_kind) {
+    case QCMG_INTER_NONE: node_inter<QCMG_INTER_NONE>(H, x, y, accumulate, gc); break;
+    case QCMG_INTER_ONSITE: node_inter<QCMG_INTER_ONSITE>(H, x, y, accumulate, gc); break;
+    default: node_inter<QCMG_INTER_GENERAL>(H, x, y, accumulate, gc); break;
+  }
+}
+
 void matvec(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate) {
   if (H->dim == 0) return;
   switch (H->inter_kind) {

@@ -333,6 +333,40 @@ class Hamiltonian:
         return ev[:m].copy(), Q[: p * m].reshape(p, m).copy()
 
 
+def lanczos_batch(hamiltonians, want_psi=False, tol=None, max_iter=None, chunk=16,
+                  raise_errors=True):
+    """Lanczos ground states of several sectors at once (qcmg_lanczos_batch):
+    each sector's recurrence runs from a captured CUDA graph of `chunk` steps
+    with its coefficients on the device, all sectors side by side; results
+    equal Hamiltonian.lanczos() on the FP64 path.  Returns a list of
+    (E0, psi or None, iterations) in the order of `hamiltonians`; a sector
+    that did not converge raises QcmgError, or with raise_errors=False each
+    entry is (E0, psi, iterations, QcmgError or None)."""
+    import ctypes
+    n = len(hamiltonians)
+    if n == 0:
+        return []
+    tol = GLOBAL["accur_lanczos"] if tol is None else tol
+    max_iter = GLOBAL["max_iter_lanczos"] if max_iter is None else max_iter
+    handles = (ctypes.c_void_p * n)(*[h._h.value for h in hamiltonians])
+    e0 = np.zeros(n)
+    nit = np.zeros(n, np.int32)
+    st = np.zeros(n, np.int32)
+    psis = [np.zeros(h.dim) if want_psi else None for h in hamiltonians]
+    pp = (ctypes.c_void_p * n)(*[(p.ctypes.data if p is not None else None) for p in psis])
+    check(lib().qcmg_lanczos_batch(n, handles, GLOBAL["seed"], tol, max_iter, chunk, ptr(e0),
+                                   ptr(nit), pp, ptr(st)))
+    if raise_errors:
+        for k in range(n):
+            check(int(st[k]))
+        return [(float(e0[k]), psis[k], int(nit[k])) for k in range(n)]
+    errs = [None if st[k] == 0 else QcmgError(int(st[k]), "sector %d of the batch: %s"
+                                              % (k, "no convergence" if st[k] == -4
+                                                 else "numerical breakdown"))
+            for k in range(n)]
+    return [(float(e0[k]), psis[k], int(nit[k]), errs[k]) for k in range(n)]
+
+
 def apply_c(L, orb, pm, nup, ndn, x, z=1.0):
     """c_orb (pm=-1) / c^dagger_orb (pm=+1) applied to x on the GPU."""
     spin = orb >= L
@@ -460,8 +494,22 @@ class ModelInstance:
             self._H[key] = Hamiltonian(self.model, self.values, Sector.of(nup, ndn))
         return self._H[key]
 
-    def ground_state(self):
-        """(GS energy, sector string) -- model_instance::low_energy_states."""
+    def gs_hamiltonians(self):
+        """The Hamiltonians of the target sectors that ground_state solves
+        (empty sectors left out), for solving many instances at once with
+        lanczos_batch."""
+        out = []
+        for s in self.target_sectors:
+            H = self.hamiltonian(s.nup, s.ndn)
+            if H.dim:
+                out.append(H)
+        return out
+
+    def ground_state(self, solved=None):
+        """(GS energy, sector string) -- model_instance::low_energy_states.
+        solved: optional {Hamiltonian: (E0, psi)} of the target sectors,
+        computed beforehand (lanczos_batch); the sectors' Lanczos runs are then
+        skipped and the states are selected as the reference does."""
         if self.gs_solved:
             return self.GS_energy, self._gs_string()
         E = 1.0e12
@@ -469,6 +517,12 @@ class ModelInstance:
         for s in self.target_sectors:
             H = self.hamiltonian(s.nup, s.ndn)
             if H.dim == 0:
+                continue
+            if solved is not None and H in solved:
+                e0, psi = solved[H]
+                E = min(E, e0)
+                if e0 - E <= max(MIN_GAP, 0.0):
+                    states.append(State(H.sec, e0, psi))
                 continue
             st, E = H.states(E)
             states += st
@@ -778,6 +832,8 @@ class ModelInstance:
         return G
 
     def self_energy(self, z, spin_down=False):
+        if self.gf_method == "L":
+            return self.self_energy_device([z], spin_down)[0]
         G = self.Green_function(z, spin_down)
         tc, _, _ = self.hopping_blocks(spin_down)
         S = np.linalg.inv(G) + tc
@@ -793,10 +849,47 @@ class ModelInstance:
         w = 1.0 / (zs[:, None] - d[None, :])
         return np.einsum("ik,zk,jk->zij", tcb, w, tcb.conj())
 
-    def self_energy_many(self, zs, spin_down=False):
-        """Sigma(z) for every z of zs at once: one batched Green-function
-        evaluation and one batched inverse instead of a loop over z."""
+    def self_energy_device(self, zs, spin_down=False, want_gamma=False):
+        """Sigma(z) (and Gamma(z) with want_gamma) for every z of zs in one
+        device call (qcmg_self_energy): the Q-matrices of the kept states, the
+        batched G(z), its inverse per frequency and the bath's Gamma(z) all on
+        the device.  GF_method 'L' only (the Q-matrix form)."""
+        if self.gf_method != "L":
+            raise ValueError("the device self-energy takes the Q-matrix (GF_method 'L')")
+        self.Green_function_solve()
         zs = np.atleast_1d(np.asarray(zs, np.complex128))
+        es, vs = [], []
+        for st in self.states:
+            e, v = st.gf_down if (spin_down and self.mixing & 4) else st.gf
+            es.append(e)
+            vs.append(v)
+        e = np.ascontiguousarray(np.concatenate(es), np.float64)
+        v = np.concatenate(vs, axis=1)
+        L, M = v.shape
+        tc, tcb, tb = self.hopping_blocks(spin_down)
+        nb = tb.shape[0]
+        vv = np.ascontiguousarray(v.T.astype(np.complex128)).view(np.float64).reshape(-1)
+        cb = np.ascontiguousarray(np.asarray(tcb, np.complex128).T).view(np.float64).reshape(-1)
+        eb = np.ascontiguousarray(np.diag(tb).real if nb else np.zeros(0))
+        tcc = np.ascontiguousarray(np.asarray(tc, np.complex128)).view(np.float64).reshape(-1)
+        zz = np.ascontiguousarray(zs).view(np.float64)
+        S = np.zeros(2 * L * L * len(zs))
+        Gm = np.zeros_like(S) if want_gamma else None
+        check(lib().qcmg_self_energy(L, M, ptr(e) if M else None, ptr(vv) if M else None, nb,
+                                     ptr(cb) if nb else None, ptr(eb) if nb else None, ptr(tcc),
+                                     len(zs), ptr(zz), ptr(S), ptr(Gm)))
+        S = S.view(np.complex128).reshape(len(zs), L, L)
+        if want_gamma:
+            return S, Gm.view(np.complex128).reshape(len(zs), L, L)
+        return S
+
+    def self_energy_many(self, zs, spin_down=False):
+        """Sigma(z) for every z of zs at once: on the device for the Q-matrix
+        form (self_energy_device), else one batched Green-function evaluation
+        and one batched inverse on the host."""
+        zs = np.atleast_1d(np.asarray(zs, np.complex128))
+        if self.gf_method == "L":
+            return self.self_energy_device(zs, spin_down)
         G = self.Green_function(zs, spin_down)
         if G.ndim == 2:
             G = G[None]

@@ -150,7 +150,14 @@ def test_green_function_pipeline(pg, tag):
     if CASES[tag][2]:
         for k, z in enumerate(ZS):
             assert np.max(np.abs(inst.hybridization_function(z) - g[f"hyb{k}"])) < 1e-12
-            assert np.max(np.abs(inst.self_energy(z) - g[f"sig{k}"])) < 1e-7
+            # Sigma carries G^-1: G's 1e-8 tolerance propagates as
+            # 1e-8 |G^-1|^2 (the same bound for the device path)
+            Gi = np.linalg.inv(g[f"gz{k}"])
+            tol = 1e-8 * max(1.0, np.linalg.norm(Gi, 2) ** 2)
+            assert np.max(np.abs(inst.self_energy(z) - g[f"sig{k}"])) < tol
+            S, Gm = inst.self_energy_device([z], want_gamma=True)
+            assert np.max(np.abs(S[0] - g[f"sig{k}"])) < tol
+            assert np.max(np.abs(Gm[0] - g[f"hyb{k}"])) < 1e-12
 
 
 @pytest.mark.parametrize("method", ["F", "M"])
