@@ -73,12 +73,19 @@ def test_matvec_matches_reference(pg, tag):
     assert np.max(np.abs(y2 - 1.0 - ref)) <= 1e-13 * np.max(np.abs(ref))
 
 
-@pytest.mark.parametrize("path", ["fixed_point", "fp64"])
-@pytest.mark.parametrize("tag", list(CASES))
+# The fixed-point path applies to one hop magnitude per spin: of the golden
+# cases, the chains (the ladder has t and t', the plaquette bath
+# hybridizations); the others are tested on the FP64 path only.
+LANCZOS_IDS = [("fixed_point", t) for t in ("chain8", "chain8_n7")] + [("fp64", t) for t in CASES]
+
+
+@pytest.mark.parametrize("path,tag", LANCZOS_IDS)
 def test_lanczos_ground_state(pg, tag, path):
     g = load_golden(tag)
     m, params, sec = engine_model(tag)
     H = pg.Hamiltonian(m, params, sec)
+    if path == "fixed_point":
+        assert H.fx_available()  # the id really runs the fixed-point path
     H.set_path(path == "fixed_point")
     e0, psi, al, be = H.lanczos()  # seeded start, as the reference's states()
     assert abs(e0 - g["lz_E0"]) <= 1e-10 * abs(g["lz_E0"])
