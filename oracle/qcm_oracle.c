@@ -110,17 +110,38 @@ size_t qo_halfop_build(int L, int N, int nel, const int* er, const int* ec, cons
 
 /* Density-density diagonal: sum over pairs (r, c, v) of v * n_r * n_c, with
  * spin-orbital r < L an up orbital (bit r of the up state) and r >= L a down
- * orbital (bit r-L of the down state). */
-static double pair_energy(uint32_t up, uint32_t dn, int L, int np, const int* pr, const int* pc,
-                          const double* pv) {
+ * orbital (bit r-L of the down state).  Split as e_up(up) + e_dn(dn) +
+ * cross(up, dn): pairs_side sums the pairs whose two orbitals are both of
+ * one spin (side 0 up, 1 down); cross_tables fills, for one down state, byte
+ * tables tab[g][byte] = sum of the cross pairs' v over the up orbitals set
+ * in byte g of an up state, so cross(up, dn) is ceil(L/8) lookups. */
+static double pairs_side(uint32_t b, int side, int L, int np, const int* pr, const int* pc,
+                         const double* pv) {
   double e = 0.0;
   for (int k = 0; k < np; ++k) {
     int r = pr[k], c = pc[k];
-    uint32_t br = r < L ? (up >> r) & 1u : (dn >> (r - L)) & 1u;
-    uint32_t bc = c < L ? (up >> c) & 1u : (dn >> (c - L)) & 1u;
-    if (br && bc) e += pv[k];
+    if ((r >= L) != side || (c >= L) != side) continue;
+    if (side) r -= L, c -= L;
+    if (((b >> r) & 1u) && ((b >> c) & 1u)) e += pv[k];
   }
   return e;
+}
+
+static void cross_tables(uint32_t dn, int L, int np, const int* pr, const int* pc,
+                         const double* pv, double tab[4][256]) {
+  double w[32] = {0.0};
+  for (int k = 0; k < np; ++k) {
+    int r = pr[k], c = pc[k];
+    if (r < L && c >= L && ((dn >> (c - L)) & 1u)) w[r] += pv[k];
+    if (c < L && r >= L && ((dn >> (r - L)) & 1u)) w[c] += pv[k];
+  }
+  for (int g = 0; g * 8 < L; ++g)
+    for (int byte = 0; byte < 256; ++byte) {
+      double e = 0.0;
+      for (int j = 0; j < 8 && g * 8 + j < L; ++j)
+        if ((byte >> j) & 1) e += w[g * 8 + j];
+      tab[g][byte] = e;
+    }
 }
 
 /* y += H x for the factorized sector (dim_up x dim_dn), x and y stored with
@@ -133,11 +154,16 @@ void qo_matvec(int L, uint32_t du, uint32_t dd, const uint32_t* bin_up, const ui
                const double* diag_up, const uint32_t* rp_dn, const uint32_t* col_dn,
                const double* val_dn, const double* diag_dn, int np, const int* pr, const int* pc,
                const double* pv, const double* x, double* y, int nthreads) {
+  /* up-state diagonal: one-body part plus the up-up pairs */
+  double* dup = (double*)malloc(sizeof(double) * (du ? du : 1));
+  for (uint32_t i = 0; i < du; ++i) dup[i] = diag_up[i] + pairs_side(bin_up[i], 0, L, np, pr, pc, pv);
+  const int ng = (L + 7) / 8;
 #ifdef _OPENMP
   if (nthreads < 1) nthreads = 1;
 #pragma omp parallel for schedule(dynamic, 4) num_threads(nthreads)
 #endif
   for (long a = 0; a < (long)dd; ++a) {
+    double tab[4][256];
     double* ya = y + (size_t)a * du;
     const double* xa = x + (size_t)a * du;
     for (uint32_t k = rp_dn[a]; k < rp_dn[a + 1]; ++k) {
@@ -145,14 +171,19 @@ void qo_matvec(int L, uint32_t du, uint32_t dd, const uint32_t* bin_up, const ui
       const double* xb = x + (size_t)col_dn[k] * du;
       for (uint32_t i = 0; i < du; ++i) ya[i] += t * xb[i];
     }
-    const double dda = diag_dn[a];
+    const double dda = diag_dn[a] + pairs_side(bin_dn[a], 1, L, np, pr, pc, pv);
+    cross_tables(bin_dn[a], L, np, pr, pc, pv, tab);
     for (uint32_t i = 0; i < du; ++i) {
       double acc = 0.0;
       for (uint32_t k = rp_up[i]; k < rp_up[i + 1]; ++k) acc += val_up[k] * xa[col_up[k]];
-      double d = diag_up[i] + dda + pair_energy(bin_up[i], bin_dn[a], L, np, pr, pc, pv);
+      const uint32_t u = bin_up[i];
+      double cross = 0.0;
+      for (int g = 0; g < ng; ++g) cross += tab[g][(u >> (8 * g)) & 0xffu];
+      double d = dup[i] + dda + cross;
       ya[i] += acc + d * xa[i];
     }
   }
+  free(dup);
 }
 
 /* Apply c_a (pm = -1) or c^dagger_a (pm = +1) to x in sector (nup, ndn),

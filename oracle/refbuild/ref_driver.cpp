@@ -43,6 +43,9 @@
 //   lat_varia NAME...                         -> QCM::CDMFT_variational_set (cluster 0)
 //   lat_host LABEL TAG NW w.. wt..            -> QCM::CDMFT_host (+ get_CDMFT_host)
 //   lat_dist LABEL TAG NP p..                 -> QCM::CDMFT_distance (cluster 0)
+//   lat_resid LABEL NP p.. | lat_grad LABEL NP p.. -> QCM::CDMFT_residuals / CDMFT_gradient
+//                                                (cluster 0), printed on standard output
+// SPEC "-" reads the commands from standard input and answers each with "@@".
 #include <chrono>
 #include <complex>
 #include <cstdio>
@@ -167,10 +170,21 @@ int main(int argc, char** argv) {
   qcm_model = make_shared<lattice_model>();
   QCM::global_parameter_init();
   Spec S;
-  ifstream in(argv[1]);
+  // SPEC "-": commands from standard input, each answered by a line "@@"
+  // once done (results of lat_resid / lat_grad on the line before)
+  const bool interactive = string(argv[1]) == "-";
+  ifstream fin;
+  if (!interactive) fin.open(argv[1]);
+  istream& in = interactive ? cin : fin;
   string line;
   try {
     while (getline(in, line)) {
+      struct Done {
+        bool on;
+        ~Done() {
+          if (on) cout << "@@" << endl;
+        }
+      } done{interactive};
       auto hash = line.find('#');
       if (hash != string::npos) line = line.substr(0, hash);
       istringstream ss(line);
@@ -491,6 +505,18 @@ int main(int argc, char** argv) {
         size_t d = 0;
         for (auto& row : Hh) for (auto& g : row) { d = g.r; for (size_t i = 0; i < g.r; i++) for (size_t j = 0; j < g.c; j++) out.push_back(g(i, j)); }
         put(tag, "c16", {(size_t)nw, d, d}, out.data(), out.size());
+      } else if (cmd == "lat_resid" || cmd == "lat_grad") {
+        // lat_resid / lat_grad LABEL NP p.. : QCM::CDMFT_residuals /
+        // CDMFT_gradient (cluster 0), printed on one stdout line
+        int label, np_; ss >> label >> np_;
+        vector<double> p(np_);
+        for (int i = 0; i < np_; i++) ss >> p[i];
+        vector<double> r = cmd == "lat_resid" ? QCM::CDMFT_residuals(p, 0, label)
+                                              : QCM::CDMFT_gradient(p, 0, label);
+        cout << "R " << r.size();
+        cout.precision(17);
+        for (double v : r) cout << ' ' << v;
+        cout << '\n';
       } else if (cmd == "lat_dist") {
         int label; string tag; int np; ss >> label >> tag >> np;
         vector<double> p(np);

@@ -188,3 +188,28 @@ def test_batched_groups_match_one_group(pg):
     for (x1, _, e1), (x2, _, e2) in zip(one, two):
         assert e1 is None and e2 is None, (e1, e2)
         assert np.array_equal(x1, x2)
+
+
+@pytest.mark.parametrize("fit", ["host", "device"])
+def test_fixed_point_loop_matches_the_reference_loop(pg, fit):
+    """The whole CDMFT loop against the reference's own: the 4-bath plaquette
+    iterated to the 'parameters' test (depth 2, accur 1e-6) with the fixed
+    point, each step's bath fitted to 1e-10 (tests/golden/make_cdmft_loop.py
+    ran the reference's C++ host function, residuals and gradient under
+    SciPy's trf).  Same number of steps, every iterate and the converged bath
+    within 1e-6 of the reference's."""
+    from lattice_helpers import build_lattice
+    from pyqcm_gb300.cdmft import CDMFT
+    import os
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdmft_loop_b4.npz"))
+    names = [str(v) for v in g["varia"]]
+    lm = build_lattice("lat_cdmft2x2_b4")
+    c = CDMFT(lm, names, grid=(39 * np.pi / 50, 50.0), kside=8, maxiter=int(g["maxiter"]),
+              depth=int(g["depth"]), accur=float(g["accur"]), accur_bath=float(g["accur_bath"]),
+              accur_dist=float(g["accur_dist"]), iteration="fixed_point", fit=fit)
+    x = c.run()
+    hist = np.array(c.history)
+    ref = g["history"][1:]
+    assert c.niter == int(g["iterations"]), (c.niter, int(g["iterations"]))
+    assert np.max(np.abs(hist - ref)) < 1e-6, np.max(np.abs(hist - ref), axis=1)
+    assert np.max(np.abs(x - g["x"])) < 1e-6, (x, g["x"])
