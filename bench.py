@@ -157,6 +157,22 @@ def cpu_port_timing(steps, threads):
     return BYTES_PER_STATE * S.dim / dt / 1e9, dt
 
 
+def port_calibration():
+    """The port's serial product against the reference's own serial
+    Hamiltonian_Factorized::mult_add on the same 4x4 sector and host
+    (oracle/calibrate_port.py; the reference's product is single-threaded),
+    or None when that record is absent."""
+    path = os.path.join(ROOT, "oracle", "port_calibration.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        c = json.load(f)
+    return {"port_over_reference_serial_speed": c["port_over_reference_speed"],
+            "reference_serial_s": c["reference_mult_add_s"],
+            "port_serial_s": c["port_mult_add_1thread_s"], "host": c["host"],
+            "note": "the reference's product runs on one thread"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -172,7 +188,7 @@ def run_reference(args):
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(),
             "cpu_baseline": {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample},
+                             "sample": sample, "calibration": port_calibration()},
             "e2e": {"value": gbs, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
@@ -318,7 +334,8 @@ def run_gpu(args):
         gbs, dt = cpu_port_timing(1, threads)
         line["cpu_baseline"] = {"value": gbs, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"1 full product y += H x on the same sector, "
-                                          f"{threads} threads ({dt:.2f} s)"}
+                                          f"{threads} threads ({dt:.2f} s)",
+                                "calibration": port_calibration()}
     if rank == 0:
         print(json.dumps(line))
     if world > 1:
@@ -326,9 +343,13 @@ def run_gpu(args):
 
 
 def _fp64_peak():
-    """FP64 FMA rate of the device in TFLOP/s (measured on the GB300s
-    with a probe kernel; MEASURED_PEAKS.json carries no FP64 figure)."""
-    return 1.0
+    """FP64 FMA rate of this device in TFLOP/s, measured now by the
+    library's probe (qcmg_fp64_fma_rate: eight FMA chains per thread, 8
+    blocks of 256 threads per SM)."""
+    from pyqcm_gb300 import _lib
+    r = _lib.c_double()
+    _lib.check(_lib.lib().qcmg_fp64_fma_rate(_lib.ctypes.byref(r)))
+    return r.value
 
 
 def run_lanczos(args):
@@ -417,6 +438,51 @@ def _vca_3x4():
     return lm
 
 
+def _lattice_oracle():
+    """The CPU oracle of the lattice layer (the CPU-baseline legs only)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import lattice_oracle
+    import qcm_oracle
+    qcm_oracle.build()
+    return lattice_oracle
+
+
+def _cpu_cluster(lm, spins, threads):
+    """The oracle's cluster solve of a lattice model's cluster: (lattice
+    oracle module, E0, {spin_down: (e, v)}, {spin_down: (tc, tcb, eb)})."""
+    lo = _lattice_oracle()
+    lm.finalize()
+    cm, vals = lm.cluster, lm.cluster_values()
+    e0, Q = lo.cluster_lehmann(cm.operators, vals, cm.n_orb, cm.n_sites, lm.target_sectors, spins,
+                               threads)
+    blocks = {sd: lo.one_body_blocks(cm.operators, vals, cm.n_orb, cm.n_sites, sd) for sd in spins}
+    return lo, e0, Q, blocks
+
+
+def cpu_sef_baseline(w, wt, threads, sample=32):
+    """The VCA Potthoff functional of the 3x4 case on the CPU oracle: the
+    cluster solve in full (Lanczos, band-Lanczos Q-matrices of both spins),
+    the 128x128 k grid integral on `sample` of the frequencies, scaled to
+    all of them."""
+    import numpy as np
+    lm = _vca_3x4()
+    t0 = time.perf_counter()
+    lo, _, Q, blocks = _cpu_cluster(lm, (False, True), threads)
+    t_solve = time.perf_counter() - t0
+    idx = np.unique(np.linspace(0, len(w) - 1, sample).round().astype(int))
+    t1 = time.perf_counter()
+    for sd in (False, True):
+        R, els, hdiff, _ = lm.fourier(sd)
+        _, tcb, eb = blocks[sd]
+        B, ldg = lo.base([(Q[sd][0], Q[sd][1], 1.0)], tcb, eb, hdiff, 1j * w[idx])
+        lo.sef_grid(B, ldg, wt[idx], R, els, (128, 128, 1), threads)
+    t_grid = (time.perf_counter() - t1) * len(w) / len(idx)
+    return {"value": t_solve + t_grid, "unit": "s", "cores": threads, "kind": "port",
+            "cluster_solve_s": t_solve, "grid_s": t_grid,
+            "sample": f"the cluster solve in full; the 128x128 k integral of both spins on "
+                      f"{len(idx)} of the {len(w)} frequencies, scaled to all"}
+
+
 def run_sef(args):
     """VCA Potthoff functional on the 128x128 k grid x 256 Gauss-Legendre
     frequencies (2 spins, 12x12 blocks): the cluster solve (ground state +
@@ -442,14 +508,21 @@ def run_sef(args):
     L = 12
     points = 128 * 128 * len(w) * len(blocks)
     flops = points * (8 * L ** 3 + 8 * L ** 3 / 3)  # per-point count of the reference's integrand
-    print(json.dumps({"metric": "vca_sef_s_per_M_value", "value": t_total, "unit": "s",
-                      "higher_is_better": False, "omega": omega, "sef_grid_s": t_grid,
-                      "points": points, "points_per_s": points / t_grid,
-                      "alg_tflops": flops / t_grid / 1e12,
-                      "fp64_peak_tflops": _fp64_peak(),
-                      "dtype": "f64", "data": "synthetic",
-                      "config": {"workload": "3x4 cluster t=1 t'=-0.3 U=8 mu=4 M_1=0.1, sector "
-                                             "R0:N12:S0, 128x128 k x 256 frequencies, 2 spins"}}))
+    lu = points * 8 * L ** 3 / 3  # executed FP64 flops of one complex LU per point
+    peak = _fp64_peak()
+    line = {"metric": "vca_sef_s_per_M_value", "value": t_total, "unit": "s",
+            "higher_is_better": False, "omega": omega, "sef_grid_s": t_grid,
+            "points": points, "points_per_s": points / t_grid,
+            "alg_tflops": flops / t_grid / 1e12,
+            "lu_tflops": lu / t_grid / 1e12, "fp64_peak_tflops": peak,
+            "lu_frac_of_fp64": lu / t_grid / 1e12 / peak,
+            "fp64_peak_kind": "measured now (qcmg_fp64_fma_rate)",
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "3x4 cluster t=1 t'=-0.3 U=8 mu=4 M_1=0.1, sector "
+                                   "R0:N12:S0, 128x128 k x 256 frequencies, 2 spins"}}
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_sef_baseline(w, wt, os.cpu_count() or 1)
+    print(json.dumps(line))
 
 
 def run_cpt(args):
@@ -479,13 +552,31 @@ def run_cpt(args):
         A = inst.spectral_function(w, k, eta=0.1)
         times.append(time.perf_counter() - t1)
     t_map = float(np.median(times))
-    print(json.dumps({"metric": "cpt_spectral_map_s", "value": t_map, "unit": "s",
-                      "higher_is_better": False, "with_cluster_solve_s": t_first,
-                      "repeats": len(times), "min_s": min(times),
-                      "points": int(A.size), "points_per_s": A.size / t_map,
-                      "dtype": "f64", "data": "synthetic",
-                      "config": {"workload": "8-site chain t=1 U=4 mu=2, 256 k x 512 w in [-8,8], "
-                                             "eta=0.1"}}))
+    line = {"metric": "cpt_spectral_map_s", "value": t_map, "unit": "s",
+            "higher_is_better": False, "with_cluster_solve_s": t_first,
+            "repeats": len(times), "min_s": min(times),
+            "points": int(A.size), "points_per_s": A.size / t_map,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "8-site chain t=1 U=4 mu=2, 256 k x 512 w in [-8,8], "
+                                   "eta=0.1"}}
+    if not args.no_cpu_baseline:
+        # the same map on the CPU oracle (cluster solve timed apart, as the
+        # repeated maps above reuse the solved cluster)
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        lo, _, Q, blocks = _cpu_cluster(lm, (False,), threads)
+        t_solve = time.perf_counter() - t0
+        R, els, hdiff, gpos = lm.fourier(False)
+        _, tcb, eb = blocks[False]
+        t1 = time.perf_counter()
+        B, _ = lo.base([(Q[False][0], Q[False][1], 1.0)], tcb, eb, hdiff, w + 0.1j)
+        g = lo.cpt(B, R, els, k @ lm.S.T, gpos, threads)
+        t_cpu = time.perf_counter() - t1
+        line["cpu_baseline"] = {"value": t_cpu, "unit": "s", "cores": threads, "kind": "port",
+                                "cluster_solve_s": t_solve,
+                                "max_abs_diff": float(np.max(np.abs(-g.imag - A))),
+                                "sample": "the whole map (256 k x 512 w)"}
+    print(json.dumps(line))
 
 
 def cdmft_instances(n, n_bath, seed=0, n_hyb=None):
@@ -502,6 +593,40 @@ def cdmft_instances(n, n_bath, seed=0, n_hyb=None):
         tb = rng.uniform(0, 1, n_hyb or n_bath)
         out.append((U, mu, eb, tb))
     return out
+
+
+def cpu_cdmft_baseline(nb, hyb, sector, names, seed, mean_iterations, threads):
+    """One CDMFT iteration of the first instance on the CPU oracle: the
+    impurity ground state and band-Lanczos Q-matrix, the host function on the
+    64x64 k grid x 200 Matsubara frequencies, the SciPy trf bath fit; points
+    per hour at the GPU run's mean iterations per point."""
+    import numpy as np
+    from pyqcm_gb300.cdmft import plaquette_bath_model
+    U, mu, eb, tb = cdmft_instances(1, nb, seed=seed, n_hyb=hyb * nb)[0]
+    lm = plaquette_bath_model(nb, sector, hybridizations=hyb)
+    params = {"t": 1.0, "tp": 0.0, "U": U, "mu": mu}
+    params.update({n: float(v) for n, v in zip(names, np.concatenate([eb, tb]))})
+    lm.set_parameters(params)
+    wn = np.array([(2 * n + 1) * np.pi / 50.0 for n in range(200)])
+    t0 = time.perf_counter()
+    lo, _, Q, blocks = _cpu_cluster(lm, (False,), threads)
+    t_solve = time.perf_counter() - t0
+    R, els, hdiff, _ = lm.fourier(False)
+    _, tcb, ebd = blocks[False]
+    host = lo.cdmft_host([(Q[False][0], Q[False][1], 1.0)], tcb, ebd, hdiff, R, els, wn, 64,
+                         lm.dim, threads)
+    t_host = time.perf_counter() - t0 - t_solve
+    cm, vals = lm.cluster, lm.cluster_values()
+    cnames = [n[:-2] for n in names]
+    lo.bath_fit(cm.operators, vals, cnames, cm.n_orb, cm.n_sites, host, wn, np.ones(len(wn)),
+                [vals[n] for n in cnames])
+    t_iter = time.perf_counter() - t0
+    return {"value": 3600.0 / (t_iter * mean_iterations), "unit": "points/h", "cores": threads,
+            "kind": "port", "s_per_iteration": t_iter, "impurity_s": t_solve, "host_s": t_host,
+            "fit_s": t_iter - t_solve - t_host,
+            "sample": f"one CDMFT iteration of instance 0 (impurity solve, host function, bath "
+                      f"fit), scaled by the GPU run's {mean_iterations:.2f} mean iterations per "
+                      f"point"}
 
 
 def run_cdmft(args):
@@ -538,7 +663,7 @@ def run_cdmft(args):
                      c.dist, why))
     conv = [r for r in rows if r[0]]
     failures = sorted({r[6] for r in rows if not r[0]})
-    print(json.dumps({
+    line = {
         "metric": "cdmft_converged_points_per_hour", "value": len(conv) / total * 3600.0,
         "unit": "points/h", "higher_is_better": True, "samples": len(rows),
         "converged": len(conv), "mean_iterations": float(np.mean([r[1] for r in rows])),
@@ -554,7 +679,12 @@ def run_cdmft(args):
         "config": {"workload": f"2x2 plaquette + {nb} bath orbitals ({nb} energies, {hyb * nb} "
                                f"hybridizations), sector {sector}, 200 Matsubara frequencies "
                                f"(beta=50), 64x64 k grid, Broyden CDMFT to the parameters test (1e-4)",
-                   "instances": "seeded U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}))
+                   "instances": "seeded U~U[0,12], mu~U[0,U], eb~U[-3,3], tb~U[0,1]"}}
+    if not args.no_cpu_baseline:
+        mean_it = float(np.mean([r[1] for r in rows]))
+        line["cpu_baseline"] = cpu_cdmft_baseline(nb, hyb, sector, names, args.seed, mean_it,
+                                                  os.cpu_count() or 1)
+    print(json.dumps(line))
 
 
 def run_lanczos_batch(args):
@@ -618,13 +748,17 @@ def run_warmstart(args):
     from pyqcm_gb300 import warmstart as ws
     torch.cuda.set_device(0)
     nb = args.bath or 8
-    path = args.warm_data or os.path.join(ROOT, "pyqcm_gb300", "data", f"warmstart_{nb}bath_train.npz")
-    P, Y = ws.load(path)
+    import glob
+    paths = (args.warm_data.split(",") if args.warm_data else sorted(glob.glob(
+        os.path.join(ROOT, "pyqcm_gb300", "data", f"warmstart_{nb}bath_train*.npz"))))
+    sets = [ws.load(p) for p in paths]
+    P, Y = np.concatenate([a for a, _ in sets]), np.concatenate([b for _, b in sets])
     t0 = time.perf_counter()
     m, loss = ws.train(P, Y, epochs=args.epochs)
     t_train = time.perf_counter() - t0
     Ptest = ws.sample_params(args.samples or 512, seed=args.seed + 1000)  # held out: another seed
-    r = ws.evaluate_batched(m, Ptest, nb, accur=args.accur, groups=args.groups)
+    r = ws.evaluate_batched(m, Ptest, nb, accur=args.accur, groups=args.groups,
+                            accur_bath=args.accur_bath, accur_dist=args.accur_bath * 1e-2)
     ip, iw = np.array(r["iters_plain"]), np.array(r["iters_warm"])
     print(json.dumps({
         "metric": "cdmft_warm_start_speedup", "value": r["s_plain"] / r["s_warm"], "unit": "x",
@@ -641,8 +775,9 @@ def run_warmstart(args):
         "config": {"workload": f"2x2 plaquette + {nb} baths ({nb} energies, "
                                f"{ws.n_hyb(nb) * nb} hybridizations), MLP 4-256-256-"
                                f"{Y.shape[1]}, U in [4,12], t' in [-0.4,0], mu in [0.35U,0.5U]",
-                   "convergence": f"parameters test {args.accur:g} (Broyden), lockstep driver "
-                                  f"in {args.groups} groups"}}))
+                   "convergence": f"parameters test {args.accur:g} (Broyden), bath fits to "
+                                  f"xtol {args.accur_bath:g} / ftol {args.accur_bath * 1e-2:g}, "
+                                  f"lockstep driver in {args.groups} groups"}}))
 
 
 def main():
@@ -681,10 +816,14 @@ def main():
     ap.add_argument("--reorth", type=int, default=0,
                     help="lanczos workload: full reorthogonalization against at most this many "
                          "vectors held in HBM (0: the reference's recurrence)")
-    ap.add_argument("--warm-data", default=None, help="training set of the warm-start workload")
+    ap.add_argument("--warm-data", default=None,
+                    help="training sets of the warm-start workload, comma-separated (default: "
+                         "every pyqcm_gb300/data/warmstart_<bath>bath_train*.npz)")
     ap.add_argument("--epochs", type=int, default=20000, help="training epochs of the warm-start MLP")
-    ap.add_argument("--accur", type=float, default=1e-7,
+    ap.add_argument("--accur", type=float, default=3e-8,
                     help="warmstart: parameters test of both CDMFT runs")
+    ap.add_argument("--accur-bath", type=float, default=1e-10,
+                    help="warmstart: xtol of every bath fit of both runs (ftol 1e-2 of it)")
     args = ap.parse_args()
     global NX, NY, NEL
     NX, NY = (int(v) for v in args.cluster.split("x"))

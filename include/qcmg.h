@@ -206,6 +206,12 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
 int qcmg_lanczos_batch(int n, qcmg_hamiltonian* const* H, unsigned seed, double tol, int max_iter,
                        int chunk, double* E0, int* niter, double* const* psi, int* status);
 
+/* FP64 FMA rate of the current device in TFLOP/s: one timed launch of
+ * eight independent FMA chains per thread over 8 blocks of 256 threads per
+ * SM (after one untimed launch).  The roofline denominator of the FP64
+ * kernels; not part of the reference's interface. */
+int qcmg_fp64_fma_rate(double* tflops);
+
 /* Breakdown of the last reorthogonalized qcmg_lanczos_ground_state on H:
  * device time of the products and of the Gram-Schmidt sweeps (ms), the
  * sweeps' algorithmic bytes (16 per stored vector element per pass, two

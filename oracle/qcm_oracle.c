@@ -228,3 +228,66 @@ void qo_apply_c(int L, int a, int pm, int nup, int ndn, const double* x, double*
   free(bu2);
   free(bd2);
 }
+
+/* Vector kernels of the band Lanczos on a list of vectors, split over
+ * OpenMP threads.  Dot products are summed over 256 fixed chunks combined in
+ * order, so the results do not depend on the thread count. */
+#define QO_CHUNKS 256
+
+/* out[k] = <V[k], w>, k < m */
+void qo_multidot(int m, const double* const* V, const double* w, size_t n, double* out,
+                 int nthreads) {
+  double* part = (double*)malloc(sizeof(double) * (size_t)(m ? m : 1) * QO_CHUNKS);
+  if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int c = 0; c < QO_CHUNKS; ++c) {
+    const size_t i0 = n * (size_t)c / QO_CHUNKS, i1 = n * (size_t)(c + 1) / QO_CHUNKS;
+    for (int k = 0; k < m; ++k) {
+      double s = 0.0;
+      for (size_t i = i0; i < i1; ++i) s += V[k][i] * w[i];
+      part[(size_t)k * QO_CHUNKS + c] = s;
+    }
+  }
+  for (int k = 0; k < m; ++k) {
+    double s = 0.0;
+    for (int c = 0; c < QO_CHUNKS; ++c) s += part[(size_t)k * QO_CHUNKS + c];
+    out[k] = s;
+  }
+  free(part);
+}
+
+/* V[k] -= coef[k] w, k < m */
+void qo_sub_rank1(int m, double* const* V, const double* coef, const double* w, size_t n,
+                  int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int c = 0; c < QO_CHUNKS; ++c) {
+    const size_t i0 = n * (size_t)c / QO_CHUNKS, i1 = n * (size_t)(c + 1) / QO_CHUNKS;
+    for (int k = 0; k < m; ++k) {
+      const double a = coef[k];
+      double* v = V[k];
+      for (size_t i = i0; i < i1; ++i) v[i] -= a * w[i];
+    }
+  }
+}
+
+/* w -= sum_k coef[k] V[k], the terms subtracted in the order k = 0 .. m-1 */
+void qo_sub_combination(int m, const double* const* V, const double* coef, double* w, size_t n,
+                        int nthreads) {
+  if (nthreads < 1) nthreads = 1;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(nthreads)
+#endif
+  for (int c = 0; c < QO_CHUNKS; ++c) {
+    const size_t i0 = n * (size_t)c / QO_CHUNKS, i1 = n * (size_t)(c + 1) / QO_CHUNKS;
+    for (size_t i = i0; i < i1; ++i) {
+      double s = w[i];
+      for (int k = 0; k < m; ++k) s -= coef[k] * V[k][i];
+      w[i] = s;
+    }
+  }
+}

@@ -41,10 +41,12 @@ i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 
 
 def build():
-    """Compiles qcm_oracle.c and qcm_oracle_rng.cpp into oracle/_build."""
+    """Compiles qcm_oracle.c, lattice_oracle.c and qcm_oracle_rng.cpp into
+    oracle/_build."""
     os.makedirs(BUILD, exist_ok=True)
     so = os.path.join(BUILD, "libqcm_oracle.so")
-    srcs = [os.path.join(HERE, "qcm_oracle.c"), os.path.join(HERE, "qcm_oracle_rng.cpp")]
+    srcs = [os.path.join(HERE, "qcm_oracle.c"), os.path.join(HERE, "lattice_oracle.c"),
+            os.path.join(HERE, "qcm_oracle_rng.cpp")]
     if os.path.exists(so) and all(os.path.getmtime(so) >= os.path.getmtime(s) for s in srcs):
         return so
     objs = []
@@ -78,6 +80,25 @@ def lib():
                                  ctypes.c_int, f64p, f64p, ctypes.c_double]
         L.qo_seeded_normal.restype = None
         L.qo_seeded_normal.argtypes = [ctypes.c_size_t, ctypes.c_uint, f64p]
+        pp = ctypes.POINTER(ctypes.c_void_p)
+        for name, args in (("qo_multidot", [ctypes.c_int, pp, f64p, ctypes.c_size_t, f64p,
+                                             ctypes.c_int]),
+                           ("qo_sub_rank1", [ctypes.c_int, pp, f64p, f64p, ctypes.c_size_t,
+                                              ctypes.c_int]),
+                           ("qo_sub_combination", [ctypes.c_int, pp, f64p, f64p,
+                                                    ctypes.c_size_t, ctypes.c_int])):
+            getattr(L, name).restype = None
+            getattr(L, name).argtypes = args
+        hop = [ctypes.c_int, f64p, ctypes.c_int, i32p, i32p, i32p, f64p]
+        L.lo_sef_grid.restype = ctypes.c_double
+        L.lo_sef_grid.argtypes = ([ctypes.c_int, ctypes.c_int, f64p, f64p, f64p] + hop
+                                  + [ctypes.c_int] * 4)
+        L.lo_cpt.restype = None
+        L.lo_cpt.argtypes = ([ctypes.c_int, ctypes.c_int, f64p] + hop
+                             + [ctypes.c_int, f64p, f64p, f64p, ctypes.c_int])
+        L.lo_kmean.restype = None
+        L.lo_kmean.argtypes = ([ctypes.c_int, ctypes.c_int, f64p] + hop
+                               + [ctypes.c_int] * 3 + [ctypes.c_double, f64p, ctypes.c_int])
         _LIB = L
     return _LIB
 
@@ -251,9 +272,38 @@ def lanczos_eigenvector(mult_add, x0, alpha, beta):
     return gs
 
 
-def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_iter_BL=600):
+def _ptrs(vs):
+    a = (ctypes.c_void_p * max(len(vs), 1))(*[v.ctypes.data for v in vs])
+    return ctypes.cast(a, ctypes.POINTER(ctypes.c_void_p))
+
+
+def _multidot(vs, w, nthreads):
+    out = np.zeros(len(vs))
+    if vs:
+        lib().qo_multidot(len(vs), _ptrs(vs), w, len(w), out, nthreads)
+    return out
+
+
+def _sub_rank1(vs, coef, w, nthreads):
+    if vs:
+        lib().qo_sub_rank1(len(vs), _ptrs(vs), np.ascontiguousarray(coef, np.float64), w, len(w),
+                           nthreads)
+
+
+def _sub_combination(vs, coef, w, nthreads):
+    if vs:
+        lib().qo_sub_combination(len(vs), _ptrs(vs), np.ascontiguousarray(coef, np.float64), w,
+                                 len(w), nthreads)
+
+
+def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_iter_BL=600,
+                 nthreads=1):
     """Freund's band Lanczos as in the reference (Lanczos.hpp:214-395).
-    Returns (evalues, U, P, M) or None when no iteration was possible."""
+    Returns (evalues, U, P, M) or None when no iteration was possible.  The
+    independent dot products and updates of one step are batched (a
+    projection on the p start vectors, the in-band orthogonalization against
+    v_j, the recurrence's combination of the previous vectors) and run on
+    `nthreads` threads."""
     p = len(phi)
     pc = p
     if M0 > max_iter_BL:
@@ -269,8 +319,11 @@ def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_
         v[i] = np.array(phi[i], np.float64, copy=True)
     ev_old = 1e12
     j = 0
+    phis = [np.ascontiguousarray(f, np.float64) for f in phi]
+    # a vector is released once the band has moved past it (index below
+    # j - pc and not deflated)
     while j < M0:
-        z = np.linalg.norm(v[j])
+        z = math.sqrt(_multidot([v[j]], v[j], nthreads)[0])
         if z < accur_deflation:
             if j >= pc:
                 Idx.append(j - pc)
@@ -282,29 +335,29 @@ def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_
                 v[k] = v[k + 1]
             v[j + pc] = None
             continue
-        v[j] = v[j] * (1.0 / z)
+        v[j] *= 1.0 / z
         if j >= pc:
             t[j, j - pc] = z
-        for k in range(p):
-            P[k, j] = phi[k] @ v[j]
+        P[:, j] = _multidot(phis, v[j], nthreads)
+        band = [v[k] for k in range(j + 1, j + pc)]
+        zz = _multidot(band, v[j], nthreads)
+        _sub_rank1(band, zz, v[j], nthreads)
         for k in range(j + 1, j + pc):
-            zz = v[j] @ v[k]
-            v[k] = v[k] - zz * v[j]
             if k >= pc:
-                t[j, k - pc] = zz
+                t[j, k - pc] = zz[k - j - 1]
         w_new = np.zeros(len(v[j]))
         mult_add(v[j], w_new)
-        v[j + pc] = w_new
         k0 = j - pc if j > pc else 0
         for k in range(k0, j):
             t[k, j] = t[j, k]
-            v[j + pc] -= t[k, j] * v[k]
+        _sub_combination([v[k] for k in range(k0, j)], t[k0:j, j], w_new, nthreads)
+        v[j + pc] = w_new
         for k in Idx:
-            w = v[k] @ v[j + pc]
-            v[j + pc] -= w * v[k]
+            w = _multidot([v[k]], w_new, nthreads)[0]
+            _sub_rank1([w_new], [w], v[k], nthreads)
             t[k, j] = w
-        w = v[j] @ v[j + pc]
-        v[j + pc] -= w * v[j]
+        w = _multidot([v[j]], w_new, nthreads)[0]
+        _sub_rank1([w_new], [w], v[j], nthreads)
         t[j, j] = w
         for k in Idx:
             t[j, k] = t[k, j]
@@ -314,6 +367,8 @@ def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_
             ev_old = evt[0]
             if test < accur_band:
                 break
+        if k0 >= 1 and (k0 - 1) not in Idx:
+            v[k0 - 1] = None
         j += 1
     M = j
     if j == 0:
@@ -322,14 +377,14 @@ def band_lanczos(mult_add, phi, M0, accur_deflation=1e-7, accur_band=1e-12, max_
     return evals, U, P[:, :M], M
 
 
-def build_Q_matrix(mult_add, phi, dim):
+def build_Q_matrix(mult_add, phi, dim, nthreads=1):
     """(e, Q) with Q = P U restricted to the first p Lanczos vectors
     (Hamiltonian_base.hpp:229-254).  Q has shape (p, M)."""
     p = len(phi)
     if dim == 0 or p == 0:
         return np.zeros(0), np.zeros((p, 0))
     M = int(14 * p * math.log(1.0 * dim))
-    res = band_lanczos(mult_add, phi, M)
+    res = band_lanczos(mult_add, phi, M, nthreads=nthreads)
     if res is None:
         return np.zeros(0), np.zeros((p, 0))
     evals, U, P, M = res
@@ -374,7 +429,8 @@ def green_function(e, v, z):
     return G.T.copy()
 
 
-def qmatrix_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, orbitals, spin_down=False):
+def qmatrix_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, orbitals, spin_down=False,
+                      nthreads=1):
     """Q-matrix (e, v) of one ground state: holes then particles, as
     model_instance::build_qmatrix assembles them.  `orbitals` are the
     Green-function orbitals (0..n_sites-1); `mult_add_of(nup, ndn)` returns
@@ -390,7 +446,7 @@ def qmatrix_for_state(mult_add_of, L_orb, nup, ndn, psi, E0, orbitals, spin_down
         mult_add, dim = mult_add_of(nup2, ndn2)
         if dim == 0:
             continue
-        e, Q = build_Q_matrix(mult_add, phi, dim)
+        e, Q = build_Q_matrix(mult_add, phi, dim, nthreads)
         e = e - E0
         if pm == -1:
             e = -e

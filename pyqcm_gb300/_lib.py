@@ -59,6 +59,7 @@ SIGNATURES = {
                                           int_p, vp, vp, c_int]),
     "qcmg_lanczos_batch": (c_int, [c_int, vp, c_uint, c_double, c_int, c_int, vp, vp, vp, vp]),
     "qcmg_lanczos_last_stats": (c_int, [vp, dbl_p, dbl_p, dbl_p, int_p, int_p, int_p]),
+    "qcmg_fp64_fma_rate": (c_int, [dbl_p]),
     "qcmg_band_lanczos": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p, vp,
                                   vp, c_int]),
     "qcmg_band_lanczos_ptrs": (c_int, [vp, c_int, vp, c_int, c_int, c_double, c_double, int_p,

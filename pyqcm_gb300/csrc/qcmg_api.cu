@@ -1,5 +1,6 @@
 // C ABI entry points (declared in include/qcmg.h): argument checking, error
 // reporting, host<->device staging, and the handle lifetime.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -291,6 +292,53 @@ int qcmg_hamiltonian_halfop(const qcmg_hamiltonian* H, int spin, size_t* nnz, ui
   });
 }
 
+// y (+)= d into page-locked host memory through its device-side address
+// (zero copy: the old y is read and the new one written in one pass).
+__global__ void k_add_to_host(const double* __restrict__ d, double* __restrict__ yh, size_t n,
+                              int acc) {
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+       i += (size_t)gridDim.x * blockDim.x)
+    yh[i] = acc ? yh[i] + d[i] : d[i];
+}
+
+// cuPointerGetAttribute through the runtime's driver entry point (no link
+// against the driver library); null when the driver does not provide it.
+typedef CUresult (*PointerGetAttributeFn)(void*, CUpointer_attribute, CUdeviceptr);
+static PointerGetAttributeFn pointer_get_attribute() {
+  static PointerGetAttributeFn fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuPointerGetAttribute", &f, 12000, cudaEnableDefault,
+                                         &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess)
+      f = nullptr;
+    return reinterpret_cast<PointerGetAttributeFn>(f);
+  }();
+  return fn;
+}
+
+// Device-side address of a page-locked host buffer when all n doubles from
+// p lie inside one page-locked allocation; null otherwise (pageable or
+// device memory, a range the driver cannot report, or a buffer shorter
+// than n), and the caller then stages the copies instead.
+static double* pinned_device_address(double* p, size_t n) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  PointerGetAttributeFn get = pointer_get_attribute();
+  CUdeviceptr start = 0;
+  size_t size = 0;
+  if (!get || get(&start, CU_POINTER_ATTRIBUTE_RANGE_START_ADDR, (CUdeviceptr)(uintptr_t)p) != 0 ||
+      get(&size, CU_POINTER_ATTRIBUTE_RANGE_SIZE, (CUdeviceptr)(uintptr_t)p) != 0)
+    return nullptr;
+  const uintptr_t lo = (uintptr_t)p, hi = lo + n * sizeof(double);
+  if (lo < (uintptr_t)start || hi > (uintptr_t)start + size) return nullptr;
+  return (double*)a.devicePointer;
+}
+
 int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags) {
   return guarded([&] {
     QCMG_CHECK_ARG(H != nullptr && x != nullptr && y != nullptr, "NULL argument");
@@ -312,6 +360,23 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
       return;
     }
     H->xbuf.alloc(n);
+    if (double* yh = pinned_device_address(y, n)) {
+      // page-locked y: x is copied in, and the result goes straight into y
+      // (the old y read while the new one is written), so y crosses the
+      // link once in each direction at the same time
+      QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
+      if (fx) {
+        fx_matvec_to_host(H, H->xbuf.p, yh, acc);
+      } else {
+        H->ybuf.alloc(n);
+        matvec(H, H->xbuf.p, H->ybuf.p, false);
+        k_add_to_host<<<152 * 8, 256, 0, H->stream>>>(H->ybuf.p, yh, n, acc ? 1 : 0);
+        QCMG_CUDA(cudaGetLastError());
+      }
+      QCMG_CUDA(cudaStreamSynchronize(H->stream));
+      if (fx) fx_check_error(H);
+      return;
+    }
     H->ybuf.alloc(n);
     QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
     if (acc) QCMG_CUDA(cudaMemcpyAsync(H->ybuf.p, y, n * 8, cudaMemcpyHostToDevice, H->stream));
@@ -451,6 +516,49 @@ int qcmg_lanczos_ground_state(qcmg_hamiltonian* H, const double* x0, unsigned se
     H->last_restarts = r.restarts;
     H->last_vectors = r.vectors;
     H->last_cycle = nc;
+  });
+}
+
+// Eight independent FMA chains per thread; the values stay bounded (a < 1)
+// and the result is written only when it equals an impossible value, so the
+// chains are not removed.
+__global__ void k_fp64_fma(double* out, int iters, double a, double b) {
+  double x[8];
+  for (int k = 0; k < 8; ++k) x[k] = 1e-3 * (threadIdx.x + k);
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fma(x[k], a, b);
+  double s = 0.0;
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == -1.0) out[0] = s;
+}
+
+int qcmg_fp64_fma_rate(double* tflops) {
+  return guarded([&] {
+    QCMG_CHECK_ARG(tflops != nullptr, "NULL argument");
+    int dev = 0, sms = 0;
+    QCMG_CUDA(cudaGetDevice(&dev));
+    QCMG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    DevBuf<double> out;
+    out.alloc(1);
+    cudaStream_t s;
+    QCMG_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    cudaEvent_t e0, e1;
+    QCMG_CUDA(cudaEventCreate(&e0));
+    QCMG_CUDA(cudaEventCreate(&e1));
+    const int blocks = sms * 8, threads = 256, iters = 4096;
+    k_fp64_fma<<<blocks, threads, 0, s>>>(out.p, iters, 0.9999999, 1e-7);  // warm-up
+    QCMG_CUDA(cudaEventRecord(e0, s));
+    k_fp64_fma<<<blocks, threads, 0, s>>>(out.p, iters, 0.9999999, 1e-7);
+    QCMG_CUDA(cudaEventRecord(e1, s));
+    QCMG_CUDA(cudaEventSynchronize(e1));
+    QCMG_CUDA(cudaGetLastError());
+    float ms = 0.f;
+    QCMG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s);
+    *tflops = 2.0 * 8.0 * iters * (double)blocks * threads / (ms * 1e-3) / 1e12;
   });
 }
 

@@ -94,7 +94,7 @@ def generate(n, seed, nb=4, kside=64):
     return np.array(P), np.array(Y), np.array(its), np.array(ts)
 
 
-def _loop(prow, x0, nb, kside, maxiter, accur):
+def _loop(prow, x0, nb, kside, maxiter, accur, accur_bath=1e-6, accur_dist=1e-8):
     U, mu, tp = (float(v) for v in prow)
     names = bath_names(nb, n_hyb(nb))
     lm = plaquette_bath_model(nb, SECTORS[nb], hybridizations=n_hyb(nb))
@@ -102,7 +102,7 @@ def _loop(prow, x0, nb, kside, maxiter, accur):
     params.update({k: float(v) for k, v in zip(names, x0)})
     lm.set_parameters(params)
     return CDMFT(lm, names, grid=(399 * np.pi / 50, 50.0), kside=kside, maxiter=maxiter,
-                 accur=accur)
+                 accur=accur, accur_bath=accur_bath, accur_dist=accur_dist)
 
 
 def generate_batched(n, seed, nb=8, kside=64, maxiter=64, accur=1e-7, groups=4, workers=8):
@@ -122,23 +122,27 @@ def generate_batched(n, seed, nb=8, kside=64, maxiter=64, accur=1e-7, groups=4, 
     return P, Y, its, dt
 
 
-def evaluate_batched(mlp, P, nb=8, kside=64, maxiter=64, accur=1e-7, groups=4, workers=8):
+def evaluate_batched(mlp, P, nb=8, kside=64, maxiter=64, accur=1e-7, groups=4, workers=8,
+                     accur_bath=1e-10, accur_dist=1e-12):
     """The held-out points run twice, all loops of a run at once
     (run_batched): from the default start and from the network's prediction
     (a point whose warm run fails is rerun from the default start, its time
-    added).  Returns a dict: wall times, iterations, fallbacks, the largest
-    difference between the two runs' converged baths, prediction errors."""
+    added).  Each step's bath fit is converged tightly (accur_bath,
+    accur_dist), so that the two runs' answers can agree to 1e-6.  Returns a
+    dict: wall times, iterations, fallbacks, the largest difference between
+    the two runs' converged baths, prediction errors."""
     from .cdmft import run_batched
     preds = [canonical(p, nb) for p in mlp.predict(features(P))]
-    plain = [_loop(p, default_bath(nb), nb, kside, maxiter, accur) for p in P]
+    tight = dict(accur_bath=accur_bath, accur_dist=accur_dist)
+    plain = [_loop(p, default_bath(nb), nb, kside, maxiter, accur, **tight) for p in P]
     t0 = time.perf_counter()
     rp = run_batched(plain, workers=workers, groups=groups)
     t_plain = time.perf_counter() - t0
-    warm = [_loop(p, x0, nb, kside, maxiter, accur) for p, x0 in zip(P, preds)]
+    warm = [_loop(p, x0, nb, kside, maxiter, accur, **tight) for p, x0 in zip(P, preds)]
     t0 = time.perf_counter()
     rw = run_batched(warm, workers=workers, groups=groups)
     failed = [k for k, (_, _, e) in enumerate(rw) if e is not None]
-    redo = [_loop(P[k], default_bath(nb), nb, kside, maxiter, accur) for k in failed]
+    redo = [_loop(P[k], default_bath(nb), nb, kside, maxiter, accur, **tight) for k in failed]
     rr = run_batched(redo, workers=workers, groups=groups) if redo else []
     t_warm = time.perf_counter() - t0
     for k, r in zip(failed, rr):

@@ -27,7 +27,7 @@ from make_golden import DRIVER, _lattice_head, num  # noqa: E402
 from models import LATTICE_CASES, hubbard_cluster  # noqa: E402
 
 VARIA = ["eb1_1", "eb2_1", "eb3_1", "eb4_1", "tb1_1", "tb2_1", "tb3_1", "tb4_1"]
-TOL = {"accur": 1e-6, "accur_bath": 1e-10, "accur_dist": 1e-12, "depth": 2, "maxiter": 60}
+TOL = {"accur": 1e-8, "accur_bath": 1e-12, "accur_dist": 1e-15, "depth": 2, "maxiter": 100}
 
 
 class Driver:

@@ -193,11 +193,17 @@ def test_batched_groups_match_one_group(pg):
 @pytest.mark.parametrize("fit", ["host", "device"])
 def test_fixed_point_loop_matches_the_reference_loop(pg, fit):
     """The whole CDMFT loop against the reference's own: the 4-bath plaquette
-    iterated to the 'parameters' test (depth 2, accur 1e-6) with the fixed
-    point, each step's bath fitted to 1e-10 (tests/golden/make_cdmft_loop.py
-    ran the reference's C++ host function, residuals and gradient under
-    SciPy's trf).  Same number of steps, every iterate and the converged bath
-    within 1e-6 of the reference's."""
+    iterated with the fixed point to the 'parameters' test (depth 2, accur
+    1e-8), each step's bath fitted tightly (xtol 1e-12, ftol 1e-15; loose
+    fits stop at different points of the distance's flat directions, 1e-6
+    apart) -- tests/golden/make_cdmft_loop.py ran the reference's C++ host
+    function, residuals and gradient under SciPy's trf.  Same number of
+    steps, every iterate and the converged bath within 1e-7 of the
+    reference's: the distance function fixes the bath only to ~1e-8 in its
+    softest directions (a displacement d there changes the cost by ~d^2
+    times a small curvature, below the cost's rounding), so two exact fits
+    with different Jacobians (exact here, finite differences in the
+    reference) stop up to a few 1e-8 apart; most iterates agree to 1e-10."""
     from lattice_helpers import build_lattice
     from pyqcm_gb300.cdmft import CDMFT
     import os
@@ -211,5 +217,6 @@ def test_fixed_point_loop_matches_the_reference_loop(pg, fit):
     hist = np.array(c.history)
     ref = g["history"][1:]
     assert c.niter == int(g["iterations"]), (c.niter, int(g["iterations"]))
-    assert np.max(np.abs(hist - ref)) < 1e-6, np.max(np.abs(hist - ref), axis=1)
-    assert np.max(np.abs(x - g["x"])) < 1e-6, (x, g["x"])
+    assert np.max(np.abs(hist - ref)) < 1e-7, np.max(np.abs(hist - ref), axis=1)
+    assert np.median(np.max(np.abs(hist - ref), axis=1)) < 1e-9
+    assert np.max(np.abs(x - g["x"])) < 1e-7, (x, g["x"])

@@ -414,3 +414,40 @@ def test_multidot_against_numpy(pg):
     out2 = np.zeros(m)
     _lib.check(pg.lib().qcmg_multidot(m, ptrs.data_ptr(), w.data_ptr(), n, _lib.ptr(out2), None))
     assert np.array_equal(out, out2)  # deterministic
+
+
+@pytest.mark.parametrize("fixed_point", [True, False])
+@pytest.mark.parametrize("offset", [0, 1])
+def test_product_into_page_locked_host_vectors(pg, fixed_point, offset):
+    """Products with a page-locked host y take the zero-copy path (x copied
+    in, the result read-modify-written straight into y), pageable ones the
+    staged copies.  Both against the oracle, accumulating and not, on a
+    16-byte-aligned y and on one starting 8 bytes in (element-wise
+    accesses)."""
+    torch = _torch()
+    import models
+    from pyqcm_gb300 import _lib
+    ns, nb, ops = models.hubbard_cluster(4, 3)
+    params = {"t": 1.0, "U": 8.0, "mu": 4.0}
+    m = pg.ClusterModel(ns, nb)
+    for name, (typ, els) in ops.items():
+        if name in params:
+            m.new_operator(name, typ, els)
+    H = pg.Hamiltonian(m, params, "R0:N12:S0")
+    H.set_path(fixed_point)
+    up, dn, pr = qo.combine_terms({k: v for k, v in ops.items() if k in params}, params, ns)
+    S = qo.Sector(ns, 6, 6, up, dn, pr)
+    x = qo.seeded_start(H.dim, 7)
+    ref = S.matvec(x, nthreads=8)
+    tol = 1e-13 * np.max(np.abs(ref))
+    buf = torch.empty(H.dim + 1, dtype=torch.float64, pin_memory=True)
+    y = buf.numpy()[offset:offset + H.dim]
+    y[:] = 0.75
+    H.mult_add(x, y)
+    assert np.max(np.abs(y - 0.75 - ref)) <= tol
+    y2 = np.full(H.dim, 0.75)  # pageable: staged copies
+    H.mult_add(x, y2)
+    assert np.max(np.abs(y2 - y)) <= tol
+    y[:] = 3.0  # y = H x overwrites
+    _lib.check(_lib.lib().qcmg_matvec(H._h, _lib.ptr(x), _lib.ptr(y), 0))
+    assert np.max(np.abs(y - ref)) <= tol
