@@ -210,9 +210,13 @@ def test_fixed_point_loop_matches_the_reference_loop(pg, fit):
     g = np.load(os.path.join(os.path.dirname(__file__), "golden", "cdmft_loop_b4.npz"))
     names = [str(v) for v in g["varia"]]
     lm = build_lattice("lat_cdmft2x2_b4")
+    # the device fit converges on the gradient (ftol 0: Gauss-Newton finish);
+    # its damped steps alone stop at the cost's rounding, ~1e-8 away along
+    # the soft directions, and the loop then jitters at its 1e-8 test
+    ftol = float(g["accur_dist"]) if fit == "host" else 0.0
     c = CDMFT(lm, names, grid=(39 * np.pi / 50, 50.0), kside=8, maxiter=int(g["maxiter"]),
               depth=int(g["depth"]), accur=float(g["accur"]), accur_bath=float(g["accur_bath"]),
-              accur_dist=float(g["accur_dist"]), iteration="fixed_point", fit=fit)
+              accur_dist=ftol, iteration="fixed_point", fit=fit)
     x = c.run()
     hist = np.array(c.history)
     ref = g["history"][1:]
