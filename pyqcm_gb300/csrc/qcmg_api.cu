@@ -318,16 +318,17 @@ static PointerGetAttributeFn pointer_get_attribute() {
 }
 
 // Device-side address of a page-locked host buffer when all n doubles from
-// p lie inside one page-locked allocation; null otherwise (pageable or
-// device memory, a range the driver cannot report, or a buffer shorter
-// than n), and the caller then stages the copies instead.
-static double* pinned_device_address(double* p, size_t n) {
+// p lie inside one page-locked allocation made or registered against
+// `device`; null otherwise (pageable or device memory, another device's
+// allocation, a range the driver cannot report, or a buffer shorter than
+// n), and the caller then stages the copies instead.
+static double* pinned_device_address(double* p, size_t n, int device) {
   cudaPointerAttributes a;
   if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
     cudaGetLastError();
     return nullptr;
   }
-  if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+  if (a.type != cudaMemoryTypeHost || !a.devicePointer || a.device != device) return nullptr;
   PointerGetAttributeFn get = pointer_get_attribute();
   CUdeviceptr start = 0;
   size_t size = 0;
@@ -360,7 +361,7 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
       return;
     }
     H->xbuf.alloc(n);
-    if (double* yh = pinned_device_address(y, n)) {
+    if (double* yh = pinned_device_address(y, n, H->device)) {
       // page-locked y: x is copied in, and the result goes straight into y
       // (the old y read while the new one is written), so y crosses the
       // link once in each direction at the same time
