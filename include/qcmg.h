@@ -435,7 +435,9 @@ int qcmg_mlp_forward(qcmg_mlp* mlp, int batch, const float* x, float* y);
 int qcmg_mlp_loss_grad(qcmg_mlp* mlp, int batch, const float* x, const float* t, float* loss,
                        float* grad);
 /* Adam (beta1 0.9, beta2 0.999, eps 1e-8) over `epochs` shuffled passes of
- * minibatches of `batch` rows; *final_loss = mean loss of the last epoch. */
+ * minibatches of `batch` rows, the learning rate annealed from lr to 0 along
+ * half a cosine over the run's steps; *final_loss = mean loss of the last
+ * epoch. */
 int qcmg_mlp_train(qcmg_mlp* mlp, int n, const float* x, const float* t, int epochs, int batch,
                    float lr, unsigned seed, float* final_loss);
 

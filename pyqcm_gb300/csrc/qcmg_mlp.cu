@@ -404,6 +404,10 @@ int qcmg_mlp_train(qcmg_mlp* M, int n, const float* x, const float* t, int epoch
     std::vector<int> perm(n);
     std::iota(perm.begin(), perm.end(), 0);
     const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
+    // the learning rate decays from lr to 0 along half a cosine over the
+    // run's minibatch steps
+    const double steps = (double)epochs * (n / batch);
+    long long k = 0;
     double last = 0.0;
     for (int e = 0; e < epochs; ++e) {
       std::shuffle(perm.begin(), perm.end(), rng);
@@ -422,8 +426,9 @@ int qcmg_mlp_train(qcmg_mlp* M, int n, const float* x, const float* t, int epoch
         ++M->step;
         const float c1 = 1.f / (1.f - std::pow(b1, (float)M->step));
         const float c2 = 1.f / (1.f - std::pow(b2, (float)M->step));
+        const float lr_k = (float)(lr * 0.5 * (1.0 + std::cos(M_PI * (double)k++ / steps)));
         k_adam<<<grid_for(M->np), 256, 0, M->s>>>(M->p.p, M->g.p, M->m.p, M->v.p, M->pb.p, M->np,
-                                                   lr, b1, b2, eps, c1, c2);
+                                                   lr_k, b1, b2, eps, c1, c2);
         QCMG_CUDA(cudaGetLastError());
       }
       last = cnt ? tot / cnt : 0.0;
