@@ -232,7 +232,7 @@ def run_gpu(args):
             ey[0] = H.matvec_fx_device(qx.data_ptr(), E.value, mb.value, qy.data_ptr(),
                                        asynchronous=True, Ey_in=ey[0])
         y = qy
-        kernels = ["k_fx_passU4", "k_fx_passD4"]
+        kernels = ["k_fx_passU4", "k_fx_passD5"]
     else:
         y = x.clone()
         step = lambda: H.matvec_device(x.data_ptr(), y.data_ptr(), asynchronous=True, accumulate=True)

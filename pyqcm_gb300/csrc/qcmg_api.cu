@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdio>
+#include <cstdlib>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -361,33 +363,61 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
       return;
     }
     H->xbuf.alloc(n);
+    // QCMG_VERBOSE: which form ran, and its phases timed with events
+    static const bool verbose = std::getenv("QCMG_VERBOSE") != nullptr;
+    cudaEvent_t ev[4] = {};
+    if (verbose)
+      for (auto& e : ev) QCMG_CUDA(cudaEventCreate(&e));
+    auto mark = [&](int i) {
+      if (verbose) QCMG_CUDA(cudaEventRecord(ev[i], H->stream));
+    };
+    auto report = [&](const char* form) {
+      if (!verbose) return;
+      float a = 0.f, b = 0.f, c = 0.f;
+      cudaEventElapsedTime(&a, ev[0], ev[1]);
+      cudaEventElapsedTime(&b, ev[1], ev[2]);
+      cudaEventElapsedTime(&c, ev[2], ev[3]);
+      std::fprintf(stderr, "qcmg_matvec: %s, x in %.3f ms, product %.3f ms, y %.3f ms\n", form, a, b,
+                   c);
+      for (auto& e : ev) cudaEventDestroy(e);
+    };
     if (double* yh = pinned_device_address(y, n, H->device)) {
       // page-locked y: x is copied in, and the result goes straight into y
       // (the old y read while the new one is written), so y crosses the
       // link once in each direction at the same time
+      mark(0);
       QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
+      mark(1);
       if (fx) {
-        fx_matvec_to_host(H, H->xbuf.p, yh, acc);
+        fx_matvec_to_host(H, H->xbuf.p, yh, acc, verbose ? ev[2] : nullptr);
       } else {
         H->ybuf.alloc(n);
         matvec(H, H->xbuf.p, H->ybuf.p, false);
+        mark(2);
         k_add_to_host<<<152 * 8, 256, 0, H->stream>>>(H->ybuf.p, yh, n, acc ? 1 : 0);
         QCMG_CUDA(cudaGetLastError());
       }
+      mark(3);
       QCMG_CUDA(cudaStreamSynchronize(H->stream));
       if (fx) fx_check_error(H);
+      report("zero-copy y");
       return;
     }
     H->ybuf.alloc(n);
+    mark(0);
     QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
     if (acc) QCMG_CUDA(cudaMemcpyAsync(H->ybuf.p, y, n * 8, cudaMemcpyHostToDevice, H->stream));
+    mark(1);
     if (fx)
       fx_matvec_f64(H, H->xbuf.p, H->ybuf.p, acc);
     else
       matvec(H, H->xbuf.p, H->ybuf.p, acc);
+    mark(2);
     QCMG_CUDA(cudaMemcpyAsync(y, H->ybuf.p, n * 8, cudaMemcpyDeviceToHost, H->stream));
+    mark(3);
     QCMG_CUDA(cudaStreamSynchronize(H->stream));
     if (fx) fx_check_error(H);
+    report("staged copies");
   });
 }
 

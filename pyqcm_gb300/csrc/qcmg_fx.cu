@@ -529,12 +529,14 @@ void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumul
 // y_host (+)= H x for x on the device and y in page-locked host memory (its
 // device-side address yh): H x in fixed point, then one pass that converts
 // and accumulates into the host vector.
-void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate) {
+void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate,
+                       cudaEvent_t product_done) {
   FxTables& T = H->fx;
   cudaStream_t s = H->stream;
   const size_t n = H->dim;
   fx_from_f64(x, n, T.x, s, T.tmp);
   fx_matvec(H, T.x, T.y, nullptr, 0.0);
+  if (product_done) QCMG_CUDA(cudaEventRecord(product_done, s));
   const unsigned g = 152u * 8u;
   if (((uintptr_t)yh & 15u) == 0)
     k_fx_to_host<true><<<g, 256, 0, s>>>(T.y.buf.p, yh, n, T.y.E, T.y.c, accumulate ? 1 : 0);

@@ -32,8 +32,10 @@ void fx_check_error(qcmg_hamiltonian* H);
 // y (+)= H x on FP64 device vectors through the fixed-point product.
 void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
 // y (+)= H x with x on the device and y in page-locked host memory, written
-// through its device-side address yh (zero copy)
-void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate);
+// through its device-side address yh (zero copy); product_done (optional) is
+// recorded between the product and the pass into y
+void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate,
+                       cudaEvent_t product_done = nullptr);
 LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, int max_iter,
                          double* psi_dev);
 
