@@ -109,7 +109,12 @@ int qcmg_hamiltonian_halfop(const qcmg_hamiltonian* H, int spin, size_t* nnz, ui
  * Replaces Hamiltonian_Factorized::mult_add
  * (src_ed/Hamiltonian/Hamiltonian_Factorized.hpp:50-58) with
  * HS_factorized_operator::multiply_add (HS_factorized_operator.hpp:57-84)
- * and HS_interaction_operator::multiply_add (HS_interaction_operator.hpp:62-70). */
+ * and HS_interaction_operator::multiply_add (HS_interaction_operator.hpp:62-70).
+ * Host vectors (no QCMG_DEVICE_PTRS): x is copied to the device; when all of
+ * y lies in one page-locked allocation of the handle's device, the result
+ * is read-modify-written into y in host memory by the device (zero copy),
+ * otherwise y is staged through device memory.  QCMG_VERBOSE in the
+ * environment prints the form taken and its phase times on stderr. */
 int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags);
 
 /* Chooses the arithmetic of the handle's products and Lanczos runs:
