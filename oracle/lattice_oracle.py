@@ -173,3 +173,18 @@ def bath_fit(ops, values, names, n_orb, n_sites, host, wn, weights, x0, spin_dow
 
     return scipy.optimize.least_squares(resid, np.asarray(x0, np.float64), method="trf",
                                         xtol=xtol, ftol=ftol, gtol=1e-12).x
+
+
+def cdmft_distance(ops, values, names, x, n_orb, n_sites, host, wn, weights, normal=True,
+                   spin_down=False):
+    """The CDMFT distance at bath x: sum_w weight |Gamma(i w; x) + G_host(i w)|^2
+    dw / dim^2, doubled for normal mixing (src_qcm/CPT.cpp:519-555)."""
+    vals = dict(values)
+    vals.update(zip(names, x))
+    _, tcb, eb = one_body_blocks(ops, vals, n_orb, n_sites, spin_down)
+    wn = np.asarray(wn, np.float64)
+    d = gamma(tcb, eb, 1j * wn) + host
+    dist = float(np.sum(np.asarray(weights)[:, None, None] * np.abs(d) ** 2))
+    if normal:
+        dist *= 2.0
+    return dist * (wn[1] - wn[0]) / (host.shape[1] ** 2)

@@ -97,3 +97,10 @@ def test_cdmft_host_function():
     G = lo.green(e, v, 1j * wn)
     host = np.linalg.inv(P) - np.linalg.inv(G) - lo.gamma(tcb, eb, 1j * wn)
     assert np.max(np.abs(host - g["host"])) < 1e-8, np.max(np.abs(host - g["host"]))
+    # the distance at two bath points against the reference's CDMFT_distance
+    # on its own host function
+    cm, vals = lm.cluster, lm.cluster_values()
+    for key, x in (("dist0", (-1.0, 1.0, 0.5)), ("dist1", (-1.2, 0.8, 0.45))):
+        d = lo.cdmft_distance(cm.operators, vals, ["eb1", "eb2", "tb1"], x, cm.n_orb, cm.n_sites,
+                              g["host"], wn, np.ones(len(wn)))
+        assert abs(d - float(g[key])) < 1e-10 * max(1.0, abs(float(g[key]))), (key, d, g[key])
