@@ -256,6 +256,12 @@ int qcmg_hamiltonian_destroy(qcmg_hamiltonian* H) {
     if (!H) return;
     cudaSetDevice(H->device);
     if (H->stream) cudaStreamSynchronize(H->stream);
+    if (H->copy_stream) {
+      cudaStreamSynchronize(H->copy_stream);
+      cudaStreamDestroy(H->copy_stream);
+    }
+    if (H->ev_x) cudaEventDestroy(H->ev_x);
+    if (H->ev_y) cudaEventDestroy(H->ev_y);
     if (H->own_stream) cudaStreamDestroy(H->own_stream);
     delete H;
   });
@@ -389,7 +395,26 @@ int qcmg_matvec(qcmg_hamiltonian* H, const double* x, double* y, unsigned flags)
       QCMG_CUDA(cudaMemcpyAsync(H->xbuf.p, x, n * 8, cudaMemcpyHostToDevice, H->stream));
       mark(1);
       if (fx) {
-        fx_matvec_to_host(H, H->xbuf.p, yh, acc, verbose ? ev[2] : nullptr);
+        // While the product runs the host->device direction is idle: copy
+        // the first part of the old y then (about what the link moves in
+        // the product's time, half of y on the fixed-point path), so that
+        // part of y only has to go out at the end.
+        size_t m = 0;
+        if (acc) {
+          m = (n / 2) & ~(size_t)1;
+          if (!H->copy_stream) {
+            QCMG_CUDA(cudaStreamCreateWithFlags(&H->copy_stream, cudaStreamNonBlocking));
+            QCMG_CUDA(cudaEventCreateWithFlags(&H->ev_x, cudaEventDisableTiming));
+            QCMG_CUDA(cudaEventCreateWithFlags(&H->ev_y, cudaEventDisableTiming));
+          }
+          H->ybuf.alloc(n);
+          QCMG_CUDA(cudaEventRecord(H->ev_x, H->stream));  // after x: no contention for the link
+          QCMG_CUDA(cudaStreamWaitEvent(H->copy_stream, H->ev_x, 0));
+          QCMG_CUDA(cudaMemcpyAsync(H->ybuf.p, y, m * 8, cudaMemcpyHostToDevice, H->copy_stream));
+          QCMG_CUDA(cudaEventRecord(H->ev_y, H->copy_stream));
+        }
+        fx_matvec_to_host(H, H->xbuf.p, yh, acc, verbose ? ev[2] : nullptr, H->ybuf.p, m,
+                          m ? H->ev_y : nullptr);
       } else {
         H->ybuf.alloc(n);
         matvec(H, H->xbuf.p, H->ybuf.p, false);

@@ -97,19 +97,24 @@ __global__ void k_fx_to_f64(const int64_t* __restrict__ q, double* __restrict__ 
 }
 
 // y (+)= c q 2^E straight into the caller's page-locked host vector (zero
-// copy): the old y streams in while the new one streams out, both link
-// directions at once.  V2: y is 16-byte aligned, two elements per access.
+// copy).  Elements below m take their old value from ypre, a device copy
+// prefetched while the product ran, and are only written (one link
+// direction); the others are read and written in host memory (both
+// directions at once).  V2: y is 16-byte aligned and m even, two elements
+// per access.
 template <bool V2>
-__global__ void k_fx_to_host(const int64_t* __restrict__ q, double* __restrict__ yh, size_t n,
-                             int E, double c, int acc) {
+__global__ void k_fx_to_host(const int64_t* __restrict__ q, double* __restrict__ yh,
+                             const double* __restrict__ ypre, size_t m, size_t n, int E, double c,
+                             int acc) {
   const size_t step = (size_t)gridDim.x * blockDim.x;
   size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
   if (V2) {
     double2* y2 = reinterpret_cast<double2*>(yh);
+    const double2* p2 = reinterpret_cast<const double2*>(ypre);
     for (; i < n / 2; i += step) {
       double2 v = make_double2(c * fx_to_f64(q[2 * i], E), c * fx_to_f64(q[2 * i + 1], E));
       if (acc) {
-        const double2 o = y2[i];
+        const double2 o = 2 * i < m ? p2[i] : y2[i];
         v.x += o.x;
         v.y += o.y;
       }
@@ -117,12 +122,12 @@ __global__ void k_fx_to_host(const int64_t* __restrict__ q, double* __restrict__
     }
     if (blockIdx.x == 0 && threadIdx.x == 0 && (n & 1)) {
       const double v = c * fx_to_f64(q[n - 1], E);
-      yh[n - 1] = acc ? yh[n - 1] + v : v;
+      yh[n - 1] = acc ? (n - 1 < m ? ypre[n - 1] : yh[n - 1]) + v : v;
     }
   } else {
     for (; i < n; i += step) {
       const double v = c * fx_to_f64(q[i], E);
-      yh[i] = acc ? yh[i] + v : v;
+      yh[i] = acc ? (i < m ? ypre[i] : yh[i]) + v : v;
     }
   }
 }
@@ -528,20 +533,24 @@ void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumul
 
 // y_host (+)= H x for x on the device and y in page-locked host memory (its
 // device-side address yh): H x in fixed point, then one pass that converts
-// and accumulates into the host vector.
+// and accumulates into the host vector, the first m elements' old values
+// read from ypre (device) once the event ypre_ready has fired.
 void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate,
-                       cudaEvent_t product_done) {
+                       cudaEvent_t product_done, const double* ypre, size_t m,
+                       cudaEvent_t ypre_ready) {
   FxTables& T = H->fx;
   cudaStream_t s = H->stream;
   const size_t n = H->dim;
   fx_from_f64(x, n, T.x, s, T.tmp);
   fx_matvec(H, T.x, T.y, nullptr, 0.0);
   if (product_done) QCMG_CUDA(cudaEventRecord(product_done, s));
+  if (m && ypre_ready) QCMG_CUDA(cudaStreamWaitEvent(s, ypre_ready, 0));
   const unsigned g = 152u * 8u;
-  if (((uintptr_t)yh & 15u) == 0)
-    k_fx_to_host<true><<<g, 256, 0, s>>>(T.y.buf.p, yh, n, T.y.E, T.y.c, accumulate ? 1 : 0);
+  const int acc = accumulate ? 1 : 0;
+  if (((uintptr_t)yh & 15u) == 0 && (m % 2) == 0)
+    k_fx_to_host<true><<<g, 256, 0, s>>>(T.y.buf.p, yh, ypre, m, n, T.y.E, T.y.c, acc);
   else
-    k_fx_to_host<false><<<g, 256, 0, s>>>(T.y.buf.p, yh, n, T.y.E, T.y.c, accumulate ? 1 : 0);
+    k_fx_to_host<false><<<g, 256, 0, s>>>(T.y.buf.p, yh, ypre, m, n, T.y.E, T.y.c, acc);
   QCMG_CUDA(cudaGetLastError());
 }
 

@@ -33,9 +33,12 @@ void fx_check_error(qcmg_hamiltonian* H);
 void fx_matvec_f64(qcmg_hamiltonian* H, const double* x, double* y, bool accumulate);
 // y (+)= H x with x on the device and y in page-locked host memory, written
 // through its device-side address yh (zero copy); product_done (optional) is
-// recorded between the product and the pass into y
+// recorded between the product and the pass into y.  With m > 0, the old
+// values of y's first m elements are read from ypre on the device (a
+// prefetched copy, complete once ypre_ready fires) instead of host memory.
 void fx_matvec_to_host(qcmg_hamiltonian* H, const double* x, double* yh, bool accumulate,
-                       cudaEvent_t product_done = nullptr);
+                       cudaEvent_t product_done = nullptr, const double* ypre = nullptr,
+                       size_t m = 0, cudaEvent_t ypre_ready = nullptr);
 LanczosResult fx_lanczos(qcmg_hamiltonian* H, const double* x0_dev, double tol, int max_iter,
                          double* psi_dev);
 

@@ -161,8 +161,11 @@ struct qcmg_hamiltonian {
   double max_inter_abs = 0.0;
   cudaStream_t stream = nullptr;      // stream the handle launches on
   cudaStream_t own_stream = nullptr;  // created with the handle
-  // staging for host-pointer calls
+  // staging for host-pointer calls; the copy stream and its events prefetch
+  // the old y while the product runs (created on first use)
   qcmg::DevBuf<double> xbuf, ybuf;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_x = nullptr, ev_y = nullptr;
   // the seeded Lanczos start vector of the last seed used (generated once)
   qcmg::DevBuf<double> seed_vec;
   unsigned seed_key = 0;
