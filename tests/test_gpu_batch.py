@@ -69,3 +69,33 @@ def test_batch_reports_no_convergence(pg):
     secs = _sectors(pg)[:2]
     with pytest.raises(pg.QcmgError):
         pg.lanczos_batch([h for _, h in secs], tol=1e-12, max_iter=5, chunk=4)
+
+
+def test_batch_over_every_sector_of_an_impurity(pg):
+    """Every (N_up >= N_dn) sector of the 2x2 plaquette with 4 bath orbitals
+    (45 sectors of 1 to 4,900 states, the empty and the full one included)
+    in one batch: bit-for-bit the single-sector recurrence, and on the
+    sectors of at most 200 states the lowest eigenvalue of the dense matrix
+    built column by column from the product (1e-10)."""
+    from pyqcm_gb300.cdmft import plaquette_bath_model
+    lm = plaquette_bath_model(4, "R0:N8:S0")
+    lm.finalize()
+    vals = {"t": 1.0, "U": 4.0, "mu": 1.7, "eb1": -1.0, "eb2": 1.1, "eb3": -0.6, "eb4": 0.7,
+            "tb1": 0.5, "tb2": 0.45, "tb3": 0.4, "tb4": 0.35}
+    no = 8
+    secs = [f"R0:N{u + d}:S{u - d}" for u in range(no + 1) for d in range(u + 1)]
+    hs = [pg.Hamiltonian(lm.cluster, vals, s) for s in secs]
+    for h in hs:
+        h.set_path(False)
+    assert min(h.dim for h in hs) == 1 and max(h.dim for h in hs) == 4900
+    res = pg.lanczos_batch(hs, tol=1e-12, max_iter=1000, chunk=16)
+    for s, h, (e0, _, nit) in zip(secs, hs, res):
+        e1, _, alpha1, _ = h.lanczos(tol=1e-12, max_iter=1000, want_psi=False)
+        assert e0 == e1 and nit == len(alpha1), (s, e0, e1, nit, len(alpha1))
+        if h.dim <= 200:
+            D = np.zeros((h.dim, h.dim))
+            for i in range(h.dim):
+                e = np.zeros(h.dim)
+                e[i] = 1.0
+                D[:, i] = h.matvec(e)
+            assert abs(np.linalg.eigvalsh(0.5 * (D + D.T))[0] - e0) < 1e-10, s
