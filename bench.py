@@ -306,14 +306,17 @@ def run_gpu(args):
     xn = xh.numpy()
     yh = torch.zeros(D, dtype=torch.float64, pin_memory=True)
     yn = yh.numpy()
-    e2e_steps = max(2, min(args.steps, 5))
+    e2e_steps = max(3, min(args.steps, 10))
     H.set_stream(0)
     H.mult_add(xn, yn)  # warm-up of the staging buffers
+    e2e_t = []
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         H.mult_add(xn, yn)
-    e2e_s = (time.perf_counter() - t0) / e2e_steps
+        e2e_t.append(time.perf_counter())
+    e2e_s = (e2e_t[-1] - t0) / e2e_steps
     e2e_val = bytes_step * world / e2e_s / 1e9
+    e2e_ms = sorted(1e3 * (b - a) for a, b in zip([t0] + e2e_t[:-1], e2e_t))
     del yh, yn
 
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
@@ -325,7 +328,9 @@ def run_gpu(args):
                          "peak_kind": peak_kind, "kernels": kernels},
             "clocks": clocks.summary(),
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": 16 * D,
-                    "d2h_bytes_per_step": 8 * D},
+                    "d2h_bytes_per_step": 8 * D, "steps": e2e_steps,
+                    "step_ms": {"min": e2e_ms[0], "median": e2e_ms[len(e2e_ms) // 2],
+                                "max": e2e_ms[-1]}},
             "gpu_launches": args.steps * len(kernels)}
     if fp64:
         line["fp64_product"] = fp64
