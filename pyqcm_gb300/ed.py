@@ -390,6 +390,24 @@ def _cuda_ready():
     return torch.cuda.is_available()
 
 
+def _concurrently(fn, args):
+    """[fn(a) for a in args], each call in a thread of its own (the engine's
+    calls release the interpreter lock and run on the handles' own streams),
+    on the caller's device; the first exception is raised once all calls are
+    done."""
+    import torch
+    from concurrent.futures import ThreadPoolExecutor
+    dev = torch.cuda.current_device()
+
+    def run(a):
+        torch.cuda.set_device(dev)
+        check(lib().qcmg_set_device(dev))
+        return fn(a)
+    with ThreadPoolExecutor(max_workers=len(args)) as ex:
+        futs = [ex.submit(run, a) for a in args]
+    return [f.result() for f in futs]
+
+
 def apply_c_device(L, orbs, pm, nup, ndn, x_dev):
     """c_orb (pm=-1) / c^dagger_orb (pm=+1) of every orbital in orbs applied
     to the device vector x_dev, on the device: a (len(orbs), dim') CUDA
@@ -555,20 +573,22 @@ class ModelInstance:
         L = self.model.n_orb
         ns = self.model.n_sites
         spin = 1 if spin_down else 0
-        blocks = {}
-        for pm in (-1, 1):
+        device = _cuda_ready()
+        psi_dev = self._psi_device(st) if device else None
+
+        def block(pm):
             nup2 = st.sec.nup + (0 if spin else pm)
             ndn2 = st.sec.ndn + (pm if spin else 0)
             if min(nup2, ndn2) < 0 or max(nup2, ndn2) > L:
-                continue
+                return None
             H = self.hamiltonian(nup2, ndn2)
             if H.dim == 0:
-                continue
-            if _cuda_ready():
+                return None
+            if device:
                 # c / c^dagger applied on the device, start vectors left there
                 e, Q = H.build_Q_matrix_device(
                     apply_c_device(L, [o + spin * L for o in range(ns)], pm, st.sec.nup,
-                                   st.sec.ndn, self._psi_device(st)))
+                                   st.sec.ndn, psi_dev))
             else:
                 phi = [apply_c(L, o + spin * L, pm, st.sec.nup, st.sec.ndn, st.psi)
                        for o in range(ns)]
@@ -579,7 +599,12 @@ class ModelInstance:
             e, Q = streamline(e, Q.astype(np.complex128))
             if pm == 1:
                 Q = Q.conj()
-            blocks[pm] = (e, Q)
+            return e, Q
+
+        # the hole and particle sectors are independent band Lanczos runs on
+        # handles of their own (own streams): on the device they run at once
+        res = _concurrently(block, (-1, 1)) if device else [block(pm) for pm in (-1, 1)]
+        blocks = {pm: r for pm, r in zip((-1, 1), res) if r is not None}
         es = [blocks[pm][0] for pm in (-1, 1) if pm in blocks]
         vs = [blocks[pm][1] for pm in (-1, 1) if pm in blocks]
         e = np.concatenate(es) if es else np.zeros(0)
@@ -610,6 +635,10 @@ class ModelInstance:
         self.ground_state()
         solve = {"F": self._cf_state, "M": self._mcf_state}.get(self.gf_method, self._qmatrix_state)
         for st in self.states:
+            if self.mixing & 4 and self.gf_method == "L" and _cuda_ready():
+                self._psi_device(st)  # uploaded once, before the two spins share it
+                st.gf, st.gf_down = _concurrently(lambda sd: solve(st, sd), (False, True))
+                continue
             st.gf = solve(st, False)
             if self.mixing & 4:
                 st.gf_down = solve(st, True)
