@@ -215,7 +215,7 @@ struct PointArgs {
   double off;       // 0 for the SEF grid, 0.5 for the CDMFT midpoint grid
   const double* gpos;  // L x 3 (CPT)
   double2* out;        // MODE 1: nw x nk;  MODE 2: partial sums
-  double* part;        // MODE 0: partial sums per block
+  double* vals;        // MODE 0: the per-point values, nw x nk
   int bpf;             // MODE 0: > 0: blocks per frequency (block b works on
                        // frequency b / bpf only, so partials never mix
                        // frequencies); 0: one flat range over all points
@@ -246,7 +246,6 @@ __global__ void k_points(PointArgs A) {
 #define MR(r, c) mr[((r) * L + (c)) * T + t]
 #define MI(r, c) mi[((r) * L + (c)) * T + t]
   const size_t npts = (size_t)A.nk * A.nw;
-  double acc = 0.0;
   // points of this block: a flat range, or (bpf > 0) the K points of one
   // frequency, strided by the frequency's blocks
   const bool per_freq = MODE == 0 && A.bpf > 0;
@@ -336,7 +335,7 @@ __global__ void k_points(PointArgs A) {
       // at high frequencies both terms are ~L log|z| and their sum is tiny,
       // so summing the large terms over K first would leave the result to
       // the rounding of that sum
-      acc += logabs + (A.ldg ? A.ldg[w] : 0.0);
+      A.vals[pt] = logabs + (A.ldg ? A.ldg[w] : 0.0);
       (void)perm;
     } else if (MODE == 1) {
       // y = M^-1 u, u_b = e^{2 pi i K.x_b};  g = (1/L) u^+ y
@@ -384,21 +383,29 @@ __global__ void k_points(PointArgs A) {
       }
     }
   }
-  if (MODE == 0) {
-    // block reduction of the log sums, fixed order, in the (now free)
-    // matrix storage: the kernel has no static shared memory, so the whole
-    // opt-in budget can hold matrices
-    __syncthreads();
-    smem[t] = acc;
-    __syncthreads();
-    if (t == 0) {
-      double s = 0.0;
-      for (int i = 0; i < T; ++i) s += smem[i];
-      A.part[blockIdx.x] = s;
-    }
-  }
 #undef MR
 #undef MI
+}
+
+// Sum of each row of vals (nrow x ncol), one block of kSumThreads per row:
+// thread t adds the elements t, t + kSumThreads, ... in order, then a fixed
+// tree adds the threads' sums.  The order depends on neither the point
+// kernel's block size nor its grid, so the Potthoff functional is the same
+// number whatever block size the tuner picks.
+constexpr int kSumThreads = 256;
+__global__ void __launch_bounds__(kSumThreads) k_row_sums(const double* __restrict__ vals,
+                                                          int ncol, double* __restrict__ sums) {
+  __shared__ double sh[kSumThreads];
+  const double* row = vals + (size_t)blockIdx.x * ncol;
+  double s = 0.0;
+  for (int i = threadIdx.x; i < ncol; i += kSumThreads) s += row[i];
+  sh[threadIdx.x] = s;
+  __syncthreads();
+  for (int h = kSumThreads / 2; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) sums[blockIdx.x] = sh[0];
 }
 
 // ---------------------------------------------------------------------------
@@ -510,7 +517,7 @@ static PointArgs point_args(const Lattice& lat, int nw) {
   A.off = 0.0;
   A.gpos = lat.gpos.p;
   A.out = nullptr;
-  A.part = nullptr;
+  A.vals = nullptr;
   A.bpf = 0;
   A.ldg = nullptr;
   A.el_start = lat.el_start.p;
@@ -559,17 +566,20 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   prepare(nw, z.data(), s);
   const double2* phases = (const double2*)phase_tables(nkx, nky, nkz, 0.0, s);
   // Several frequencies per launch (enough blocks for many waves on every
-  // SM), with each block's partial sum tied to one frequency, so the
-  // weights are still applied to whole per-frequency sums.
+  // SM), each block working on the points of one frequency; every point's
+  // log|det| is stored, and each frequency's sum is then taken in a fixed
+  // order (k_row_sums), so the weights apply to whole per-frequency sums and
+  // the result does not depend on the block size.
   auto shape = [&](int T, unsigned& bpf, int& fpl) {
     bpf = (unsigned)std::max<size_t>(1, std::min<size_t>((nk + T - 1) / T, 152 * 4));
     fpl = std::max(1, std::min(nw, (int)((152u * 16u + bpf - 1) / bpf)));
   };
-  DevBuf<double> part;
+  DevBuf<double> vals, sums;
   auto launch = [&](int T, int i0, int nf, unsigned bpf) {
     const size_t smem = (size_t)2 * L * L * T * 8;
     QCMG_CUDA(cudaFuncSetAttribute(k_points<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    (int)smem));
+    if (vals.n < (size_t)nf * nk) vals.alloc((size_t)nf * nk);
     PointArgs A = point_args(*this, nf);
     A.base = (const double2*)base.p + (size_t)i0 * L * L;
     A.nk = nk;
@@ -577,7 +587,7 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
     A.gy = nky;
     A.gz = nkz;
     A.off = 0.0;
-    A.part = part.p;
+    A.vals = vals.p;
     A.bpf = (int)bpf;
     A.ldg = logdetG.p + i0;
     A.tab = phases;
@@ -590,7 +600,6 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
         unsigned b;
         int f;
         shape(Tc, b, f);
-        if (part.n < (size_t)b * f) part.alloc((size_t)b * f);
         const int nf = std::min(f, nw);
         launch(Tc, 0, nf, b);
         return nf;
@@ -599,18 +608,16 @@ double Lattice::sef_grid(int nw, const double* w, const double* wt, int nkx, int
   unsigned bpf;
   int fpl;
   shape(T, bpf, fpl);
-  if (part.n < (size_t)bpf * fpl) part.alloc((size_t)bpf * fpl);
-  std::vector<double> hp((size_t)bpf * fpl);
+  if (sums.n < (size_t)fpl) sums.alloc((size_t)fpl);
+  std::vector<double> hs((size_t)fpl);
   for (int i0 = 0; i0 < nw; i0 += fpl) {
     const int nf = std::min(fpl, nw - i0);
     launch(T, i0, nf, bpf);
-    QCMG_CUDA(cudaMemcpyAsync(hp.data(), part.p, (size_t)bpf * nf * 8, cudaMemcpyDeviceToHost, s));
+    k_row_sums<<<nf, kSumThreads, 0, s>>>(vals.p, nk, sums.p);
+    QCMG_CUDA(cudaGetLastError());
+    QCMG_CUDA(cudaMemcpyAsync(hs.data(), sums.p, (size_t)nf * 8, cudaMemcpyDeviceToHost, s));
     QCMG_CUDA(cudaStreamSynchronize(s));
-    for (int f = 0; f < nf; ++f) {
-      double sk = 0.0;
-      for (unsigned b = 0; b < bpf; ++b) sk += hp[(size_t)f * bpf + b];
-      total += wt[i0 + f] * (sk / nk);
-    }
+    for (int f = 0; f < nf; ++f) total += wt[i0 + f] * (hs[f] / nk);
   }
   return total;
 }

@@ -184,3 +184,14 @@ def test_vca_3x4_potthoff_functional(pg):
     lat.discrete_integration_grid(g["sef_w"], g["sef_wt"])
     om = inst.Potthoff_functional()
     assert abs(om - float(g["sef"])) < 1e-8, (om, float(g["sef"]))
+    # the same number bit for bit whatever block size the point kernel runs
+    # with (the per-frequency sums are taken in a fixed order)
+    import os
+    got = []
+    for T in ("32", "64", "96"):
+        os.environ["QCMG_POINT_THREADS"] = T
+        try:
+            got.append(inst.Potthoff_functional())
+        finally:
+            del os.environ["QCMG_POINT_THREADS"]
+    assert got == [om, om, om], (got, om)
