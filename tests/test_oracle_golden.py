@@ -174,3 +174,27 @@ def test_matrix_continued_fraction_green_function_against_reference(tag):
         for k in range(len(ZS)):
             ref = gm[("gzdn" if spin_down else "gz") + str(k)]
             assert np.max(np.abs(G[k] - ref)) < 1e-10, (tag, spin_down, k, np.max(np.abs(G[k] - ref)))
+
+
+def test_band_lanczos_vector_kernels():
+    """The oracle's batched vector kernels against numpy, and the dot
+    products equal on 1 and 4 threads (fixed-chunk sums)."""
+    rng = np.random.default_rng(3)
+    n = 100_003
+    vs = [rng.standard_normal(n) for _ in range(5)]
+    w = rng.standard_normal(n)
+    d1 = qo._multidot(vs, w, 1)
+    d4 = qo._multidot(vs, w, 4)
+    assert np.array_equal(d1, d4)
+    assert np.allclose(d1, [v @ w for v in vs], rtol=1e-13, atol=1e-10)
+    coef = rng.standard_normal(5)
+    ref = [v - c * w for v, c in zip(vs, coef)]
+    got = [v.copy() for v in vs]
+    qo._sub_rank1(got, coef, w, 4)
+    assert all(np.max(np.abs(a - b)) < 1e-12 for a, b in zip(got, ref))  # FMA or not
+    y = w.copy()
+    qo._sub_combination(vs, coef, y, 4)
+    ref_y = w.copy()
+    for v, c in zip(vs, coef):
+        ref_y = ref_y - c * v
+    assert np.max(np.abs(y - ref_y)) < 1e-12
