@@ -221,7 +221,13 @@ class CDMFT:
 
     varia: lattice-level bath parameter names of cluster 1 ('eb1_1', ...).
     grid: (wc, beta) of the Matsubara grid.  kside: side of the k grid of the
-    host function.  x0: starting bath parameters (default: the model's)."""
+    host function.  x0: starting bath parameters (default: the model's).
+    fit: 'device' fits the bath with Levenberg-Marquardt on the GPU
+    (qcmg_bath_fit); 'host' with SciPy's trf on the exact Jacobian, the
+    reference's optimizer.  The distance can have several local minima, and
+    from a start far from all of them the two optimizers may end in
+    different ones (the damped steps tend to stay on the start's side); the
+    loop then converges to a different fixed point."""
 
     def __init__(self, model, varia, grid=(399 * np.pi / 50, 50.0), kside=64, maxiter=32,
                  miniter=0, depth=2, accur=1e-4, accur_bath=1e-6, accur_dist=1e-8, damping=0.0,
